@@ -1,0 +1,97 @@
+// fim_internal.h -- shared declarations of the GB300 FIM solver (host side
+// and kernels).  Not part of the C ABI.
+#pragma once
+
+#include <cstdint>
+#include <cstddef>
+
+#include <cuda_runtime.h>
+
+namespace fimgb {
+
+// Reference node states (types.h:85).
+enum : uint8_t { ST_FAR = 0, ST_NEIG = 1, ST_NARROW = 2, ST_NEXT = 3, ST_FROZEN = 4, ST_TAIL = 5 };
+
+// Kernel error codes written into FimCtl::error.
+enum : int { KERR_NONE = 0, KERR_TIMEOUT = 1, KERR_MAX_ITER = 2 };
+
+// Device control block: counters of the three rotating list slots, the grid
+// barrier, the error word and statistics.  Lives in device memory; the host
+// clears it before every launch.
+struct FimCtl {
+  int32_t n_narrow[3];      // narrow list length of the iteration using this slot
+  int32_t n_frozen[3];      // vertices frozen in that iteration
+  int32_t n_marked[3];      // neighbours re-solved in that iteration
+  uint32_t bar_count;       // grid barrier arrivals
+  uint32_t bar_gen;         // grid barrier generation
+  int32_t error;            // KERR_*
+  int32_t error_where;      // phase that failed
+  int64_t iterations;
+  int64_t vertex_updates;
+  int64_t corner_evals;
+};
+
+// Everything the persistent kernel touches, as device pointers.
+//
+// Vertices of the kernel are vertex *copies*: with submesh tags every
+// submesh holds its own copy of each of its vertices (the reference's
+// per-submesh local numbering, extract_submeshes2, types.cpp:306-570), and a
+// tet's corners only see the copies of its own submesh.  Without tags there
+// is one submesh and copy == vertex.
+struct FimDev {
+  int32_t nV;                 // vertex copies
+  int32_t nG;                 // mesh vertices
+  const int64_t *gptr;        // [nG+1] copies of each mesh vertex (nullptr: copy == vertex)
+  const int32_t *gcopy;
+  double *phi_out;            // [nG] gathered results (min over copies)
+  uint8_t *st_out;            // [nG] (max over copies)
+  int64_t nT;
+  int64_t nC;                 // corners = 4 * nT
+  // topology
+  const int64_t *cptr;        // [nV+1] corner range per vertex
+  const int4 *cids;           // [nC] other three vertices of the corner ("1","2","3"), w unused
+  const double *cgeo;         // [nC*10] e13,e23,e34,e12,e14,e24, sqrt(e14), sqrt(e24), sqrt(e34), pad
+  const int64_t *nptr;        // [nV+1] vertex neighbourhood (self included)
+  const int32_t *nbr;
+  // state
+  double *phi;                // current times
+  double *phi2;               // next times (equal to phi outside the updated lists)
+  uint8_t *st;                // state
+  uint8_t *tst;               // reference tmp_state
+  int32_t *flag;              // iteration stamp of "marked"
+  int32_t *list[3];           // rotating narrow lists
+  int32_t *lfrozen;           // frozen this iteration
+  int32_t *lmarked;           // marked this iteration
+  uint8_t *dec;               // decided state of marked vertices
+  // stimuli
+  const int32_t *seed_v;
+  const double *seed_t;
+  int32_t nseed;
+  FimCtl *ctl;
+};
+
+struct FimParams {
+  double dt;            // window length (inf = endless)
+  int32_t n_steps;
+  double front_width;   // reference wavefront width
+  double apd;           // < 0 disables the frozen->tail->far reset
+  int64_t max_iter;     // per window
+  uint64_t timeout_ns;  // per wait
+};
+
+// Records the message returned by fim_last_error(NULL) on this thread.
+void set_last_error(const char *msg);
+
+// ---- kernels (fim_kernels.cu) ----
+// FP64 metric + edge norms per tet scattered into the corner records.
+cudaError_t launch_metric(const int32_t *tslots, const int64_t *cidx, const double *xyz,
+                          const double *fib, const double *cf, const double *ct, int64_t nT,
+                          double *cgeo, cudaStream_t stream);
+// Persistent cooperative solve.
+cudaError_t launch_solve(const FimDev &d, const FimParams &p, int grid, int block, cudaStream_t stream);
+// Occupancy-derived grid size for the cooperative launch.
+cudaError_t solve_grid_size(int device, int block, int *grid);
+// Writes phi (any order) into out.
+cudaError_t launch_copy(const double *src, double *dst, int64_t n, cudaStream_t stream);
+
+}  // namespace fimgb

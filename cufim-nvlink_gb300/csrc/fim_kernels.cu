@@ -1,0 +1,542 @@
+// fim_kernels.cu -- sm_103a kernels of the GB300 FIM eikonal solver.
+//
+// This translation unit is compiled with -fmad=false and without fast-math:
+// every FP64 expression below is evaluated in the order written, with IEEE
+// round-to-nearest division and square root and no fused multiply-adds, so
+// the solver reproduces the reference's FP64 source semantics bit for bit
+// (the reference's results are chaotic in the last bits: a 1e-6 relative
+// change of the inputs moves single vertices by 1e-3 of max(t), so nothing
+// weaker than bit-exact arithmetic can match it to 1e-4).
+//
+// Kernels
+//  * fim_metric_kernel -- FP64 per-tet metric and squared edge norms
+//    (compute_velocity_tensor_f3 + compute_geo, types.h:173-188,
+//    types.cpp:227-257), written straight into the four corner records of
+//    the tet in the relabelled order the local solver reads
+//    (gray-code tables, cuda_fim.h:41-48), plus the three edge lengths.
+//  * fim_solve_kernel -- one persistent cooperative launch for the whole
+//    solve: reset + seeding (reset_states_gpu / update_events_gpu,
+//    cuda_fim.cu:479-542, 632-683), per window update_states
+//    (cuda_fim.cu:1790-1845), then FIM iterations with the phases of
+//    compute_step (cuda_fim.cu:1992-2334) as global Jacobi steps over
+//    compacted lists (narrow list, vertices frozen this iteration,
+//    neighbours to re-solve), separated by a bounded grid barrier.
+#include "fim_internal.h"
+
+#include <cfloat>
+#include <cstdint>
+
+namespace fimgb {
+
+#define FIM_INF DBL_MAX
+#define FULL_MASK 0xffffffffu
+
+// ---------------------------------------------------------------------------
+// local solver, FP64 with the reference's float-typed triangle intermediates
+
+// solve_tri_cu, cuda_fim.h:1256-1300
+__device__ __forceinline__ double tri_ref(double e12, double e13, double e23, double p1, double p2)
+{
+  const double a = e23;
+  const double b = -0.5 * (e12 + e23 - e13);
+  const double c = e12;
+  const double p12 = p2 - p1;
+  float dv = (float)(p12 * p12 - c);
+  const float sv = (float)((double)dv * (b * b - a * c));
+  if ((double)dv != 0.0 && (double)sv >= 0.0) {
+    dv = (float)(c * (double)dv);
+    const float st = sqrtf(sv);
+    const float l1 = (float)(-(b * p12 * p12 - b * c - (double)st * p12) / (double)dv);
+    const float l2 = (float)(-(b * p12 * p12 - b * c + (double)st * p12) / (double)dv);
+    float r1 = (float)(p2 - (double)l1 * p12 + sqrt(a + 2.0 * (double)l1 * b + (double)(l1 * l1) * c));
+    if (!(((double)l1 >= 0.0) && ((double)l1 <= 1.0))) r1 = (float)FIM_INF;
+    float r2 = (float)(p2 - (double)l2 * p12 + sqrt(a + 2.0 * (double)l2 * b + (double)(l2 * l2) * c));
+    if (!(((double)l2 >= 0.0) && ((double)l2 <= 1.0))) r2 = (float)FIM_INF;
+    return (double)fminf(r1, r2);
+  }
+  return FIM_INF;
+}
+
+// solve_tet_cu, cuda_fim.h:1302-1360 (the reference's closed form, term for term)
+__device__ __forceinline__ double tet_ref(double e13, double e23, double e34, double e12, double e14,
+                                          double e24, double p1, double p2, double p3)
+{
+  const double a = e13;
+  const double b = 0.5 * (e23 + e13 - e12);
+  const double c = -0.5 * (e34 + e13 - e14);
+  const double d = e23;
+  const double e = -0.5 * (e34 + e23 - e24);
+  const double f = e34;
+  const double q13 = p3 - p1;
+  const double q23 = p3 - p2;
+
+  const double sqt =
+    -e*e*c*d*d + a*d*d*d*d - (b*b*c - a*c*c)*f*f + ((b*b - a*c)*f*f -
+    (e*e*c - a*d*d - 2.*(e*c - b*d)*e)*f)*q13*q13 - 2.*(e*e*c*d -
+    2.*e*b*d*d + a*d*d*d + (b*b - a*c)*d*f)*q13*q23 + (e*e*c*c -
+    2.*e*b*c*d + a*c*d*d + (b*b*c - a*c*c)*f)*q23*q23 + 2.*(e*c*d*d -
+    b*d*d*d)*e + (e*e*c*c + (b*b - 2.*a*c)*d*d - 2.*(e*c*c - b*c*d)*e)*f;
+
+  if (sqt < 0.) return FIM_INF;
+
+  const double pa = e*c*d*d - b*d*d*d + (e*c - b*d)*f*q13*q13 - 2.*(e*c*d - b*d*d)*q13*q23 +
+                    (e*c*c - b*c*d)*q23*q23 - (e*c*c - b*c*d)*f;
+  const double pb = (d*d*d*d - 2.*c*d*d*f + c*c*f*f + (d*d*f - c*f*f)*q13*q13 -
+                     2.*(d*d*d - c*d*f)*q13*q23 + (c*d*d - c*c*f)*q23*q23);
+
+  const double la2 = (pa + sqt*(d*q13 - c*q23))/pb;
+  const double lb2 = (pa - sqt*(d*q13 - c*q23))/pb;
+  const double la1 = -((f*la2 + e)*q13 - (d*la2 + b)*q23)/(d*q13 - c*q23);
+  const double lb1 = -((f*lb2 + e)*q13 - (d*lb2 + b)*q23)/(d*q13 - c*q23);
+
+  double l3 = 1 - la1 - la2, ra = FIM_INF, rb = FIM_INF;
+  if ((la1 > 0. && la1 < 1.) && (la2 > 0. && la2 < 1.) && l3 > 0.)
+    ra = la1*p1 + la2*p2 + l3*p3 + sqrt(a + 2.*la1*b + la1*la1*c + 2.*la1*la2*d + 2.*la2*e + la2*la2*f);
+  l3 = 1 - lb1 - lb2;
+  if ((lb1 > 0. && lb1 < 1.) && (lb2 > 0. && lb2 < 1.) && l3 > 0.)
+    rb = lb1*p1 + lb2*p2 + l3*p3 + sqrt(a + 2.*lb1*b + lb1*lb1*c + 2.*lb1*lb2*d + 2.*lb2*e + lb2*lb2*f);
+  return fmin(ra, rb);
+}
+
+// update_per_element (cuda_fim.h:1362-1411) for one corner.  A branch whose
+// neighbours are not all valid is skipped: with the reference's INF
+// (DBL_MAX) operands such a branch never produces a value below the others
+// (checked against the reference's own code on 3e5 random corners), so the
+// result is identical.  g: e13,e23,e34,e12,e14,e24,sqrt(e14),sqrt(e24),sqrt(e34).
+__device__ __forceinline__ double corner_candidate(const double *g, double p1, double p2, double p3,
+                                                   bool v1, bool v2, bool v3)
+{
+  double r = FIM_INF;
+  if (v1 && v2 && v3) r = tet_ref(g[0], g[1], g[2], g[3], g[4], g[5], p1, p2, p3);
+  if (v1 && v2) r = fmin(r, tri_ref(g[3], g[4], g[5], p1, p2));
+  if (v2 && v3) r = fmin(r, tri_ref(g[1], g[5], g[2], p2, p3));
+  if (v1 && v3) r = fmin(r, tri_ref(g[0], g[4], g[2], p1, p3));
+  if (v1) r = fmin(r, p1 + g[6]);
+  if (v2) r = fmin(r, p2 + g[7]);
+  if (v3) r = fmin(r, p3 + g[8]);
+  return r;
+}
+
+// ---------------------------------------------------------------------------
+// metric kernel
+
+// Edge numbering of a tet with slots 0..3: (0,1) (0,2) (1,2) (0,3) (1,3) (2,3)
+// (types.cpp:240-245).
+__host__ __device__ constexpr int edge_index(int i, int j)
+{
+  return (i > j) ? edge_index(j, i) : (j == 1 ? 0 : (j == 2 ? (i == 0 ? 1 : 2) : 3 + i));
+}
+// For target slot t the other slots are relabelled "1","2","3" =
+// (t+1)%4, (t+2)%4, (t+3)%4 (the reference's gray-code mapping,
+// cuda_fim.h:41-48).  sel_of(t, k) is the edge index of the k-th relabelled
+// edge e13, e23, e34, e12, e14, e24.
+__host__ __device__ constexpr int sel_of(int t, int k)
+{
+  return k == 0 ? edge_index((t + 1) & 3, (t + 3) & 3)
+       : k == 1 ? edge_index((t + 2) & 3, (t + 3) & 3)
+       : k == 2 ? edge_index((t + 3) & 3, t)
+       : k == 3 ? edge_index((t + 1) & 3, (t + 2) & 3)
+       : k == 4 ? edge_index((t + 1) & 3, t)
+       :          edge_index((t + 2) & 3, t);
+}
+
+__global__ void fim_metric_kernel(const int32_t *__restrict__ tslots, const int64_t *__restrict__ cidx,
+                                  const double *__restrict__ xyz, const double *__restrict__ fib,
+                                  const double *__restrict__ cf, const double *__restrict__ ct,
+                                  int64_t nT, double *__restrict__ cgeo)
+{
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nT;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const double f0 = fib[3 * e + 0], f1 = fib[3 * e + 1], f2 = fib[3 * e + 2];
+    const double fa = f0*f0, fb = f0*f1, fc = f0*f2, fd = f1*f1, fe = f1*f2, ff = f2*f2;
+    const double vf = 1. / cf[e] / cf[e], vs = 1. / ct[e] / ct[e];
+    const double M0 = vf*fa + vs*(1. - fa);
+    const double M1 = (vf - vs)*fb;
+    const double M2 = (vf - vs)*fc;
+    const double M3 = vf*fd + vs*(1. - fd);
+    const double M4 = (vf - vs)*fe;
+    const double M5 = vf*ff + vs*(1. - ff);
+    const int32_t v0 = tslots[4 * e + 0], v1 = tslots[4 * e + 1];
+    const int32_t v2 = tslots[4 * e + 2], v3 = tslots[4 * e + 3];
+    const int32_t va[6] = {v0, v0, v1, v0, v1, v2};
+    const int32_t vb[6] = {v1, v2, v2, v3, v3, v3};
+    double g[6], s[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+      // load_edge(a, b) = x_a - x_b (types.h:210-216); aMb_sym (types.h:165-171)
+      const double ex = xyz[3 * (int64_t)va[k] + 0] - xyz[3 * (int64_t)vb[k] + 0];
+      const double ey = xyz[3 * (int64_t)va[k] + 1] - xyz[3 * (int64_t)vb[k] + 1];
+      const double ez = xyz[3 * (int64_t)va[k] + 2] - xyz[3 * (int64_t)vb[k] + 2];
+      g[k] = (M0*ex + M1*ey + M2*ez)*ex + (M1*ex + M3*ey + M4*ez)*ey + (M2*ex + M4*ey + M5*ez)*ez;
+      s[k] = sqrt(g[k]);
+    }
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      double *o = cgeo + 10 * cidx[4 * e + t];
+      o[0] = g[sel_of(t, 0)]; o[1] = g[sel_of(t, 1)]; o[2] = g[sel_of(t, 2)];
+      o[3] = g[sel_of(t, 3)]; o[4] = g[sel_of(t, 4)]; o[5] = g[sel_of(t, 5)];
+      o[6] = s[sel_of(t, 4)]; o[7] = s[sel_of(t, 5)]; o[8] = s[sel_of(t, 2)];
+      o[9] = 0.0;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// bounded grid barrier
+
+__device__ __forceinline__ uint64_t global_timer()
+{
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t *p)
+{
+  uint32_t v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ void st_release_u32(uint32_t *p, uint32_t v)
+{
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+__device__ __forceinline__ int ld_volatile_i32(const int32_t *p)
+{
+  return *(const volatile int32_t *)p;
+}
+
+// All blocks of the (co-resident) grid meet here.  Every wait is bounded by
+// timeout_ns of %globaltimer and by a spin cap; on expiry the block records
+// KERR_TIMEOUT and the phase, and every block leaves the kernel at its next
+// barrier.  Returns false when the caller must return.
+__device__ bool grid_sync(FimCtl *ctl, uint32_t nblocks, uint64_t timeout_ns, int where)
+{
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    const uint32_t gen = ld_acquire_u32(&ctl->bar_gen);
+    __threadfence();
+    const uint32_t arrived = atomicAdd(&ctl->bar_count, 1u) + 1u;
+    if (arrived == nblocks) {
+      atomicExch(&ctl->bar_count, 0u);
+      __threadfence();
+      st_release_u32(&ctl->bar_gen, gen + 1u);
+    } else {
+      const uint64_t t0 = global_timer();
+      uint32_t spins = 0;
+      while (ld_acquire_u32(&ctl->bar_gen) == gen) {
+        ++spins;
+        if ((spins & 63u) == 0u) {
+          if (ld_volatile_i32(&ctl->error) != KERR_NONE) { ok = 0; break; }
+          if (global_timer() - t0 > timeout_ns || spins > (1u << 30)) {
+            if (atomicCAS(&ctl->error, KERR_NONE, KERR_TIMEOUT) == KERR_NONE) ctl->error_where = where;
+            ok = 0;
+            break;
+          }
+        }
+        __nanosleep(64);
+      }
+    }
+    if (ok && ld_volatile_i32(&ctl->error) != KERR_NONE) ok = 0;
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+// ---------------------------------------------------------------------------
+// persistent solve
+
+struct WarpCtx {
+  int lane;
+  int64_t gwarp;
+  int64_t nwarps;
+};
+
+// New time of vertex v from all its corners (one warp, lanes over corners):
+// min over the candidates of update_per_element with the reference's
+// validity rule (state >= narrow and phi > phi_start - front_width,
+// cuda_fim.h:1375-1383).  Returns the warp-wide minimum on every lane.
+__device__ __forceinline__ double warp_vertex_update(const FimDev &d, int32_t v, double lower,
+                                                     int lane, int64_t &evals)
+{
+  const int64_t c0 = d.cptr[v], c1 = d.cptr[v + 1];
+  double best = FIM_INF;
+  for (int64_t c = c0 + lane; c < c1; c += 32) {
+    const int4 id = __ldg(d.cids + c);
+    const double p1 = __ldcg(d.phi + id.x), p2 = __ldcg(d.phi + id.y), p3 = __ldcg(d.phi + id.z);
+    const uint8_t s1 = __ldcg(d.st + id.x), s2 = __ldcg(d.st + id.y), s3 = __ldcg(d.st + id.z);
+    const bool v1 = (s1 >= ST_NARROW) && (p1 > lower);
+    const bool v2 = (s2 >= ST_NARROW) && (p2 > lower);
+    const bool v3 = (s3 >= ST_NARROW) && (p3 > lower);
+    if (v1 || v2 || v3) {
+      const double2 *gp = reinterpret_cast<const double2 *>(d.cgeo + 10 * c);
+      double g[10];
+#pragma unroll
+      for (int k = 0; k < 5; ++k) {
+        const double2 t = __ldg(gp + k);
+        g[2 * k] = t.x;
+        g[2 * k + 1] = t.y;
+      }
+      best = fmin(best, corner_candidate(g, v1 ? p1 : FIM_INF, v2 ? p2 : FIM_INF, v3 ? p3 : FIM_INF,
+                                         v1, v2, v3));
+      ++evals;
+    }
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) best = fmin(best, __shfl_xor_sync(FULL_MASK, best, off));
+  return best;
+}
+
+__global__ void __launch_bounds__(256) fim_solve_kernel(FimDev d, FimParams p)
+{
+  FimCtl *ctl = d.ctl;
+  const uint32_t nblocks = gridDim.x;
+  const int64_t gtid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
+  WarpCtx w;
+  w.lane = threadIdx.x & 31;
+  w.gwarp = gtid >> 5;
+  w.nwarps = nthreads >> 5;
+  int64_t my_evals = 0, my_updates = 0;
+  int where = 0;
+
+  // reset_states_gpu + update_events_gpu: phi = INF, far; seeds narrow.
+  for (int64_t v = gtid; v < d.nV; v += nthreads) {
+    d.phi[v] = FIM_INF; d.phi2[v] = FIM_INF; d.st[v] = ST_FAR; d.tst[v] = ST_FAR; d.flag[v] = 0;
+  }
+  if (!grid_sync(ctl, nblocks, p.timeout_ns, ++where)) return;
+  for (int64_t i = gtid; i < d.nseed; i += nthreads) {
+    const int32_t v = d.seed_v[i];
+    d.phi[v] = d.seed_t[i]; d.phi2[v] = d.seed_t[i]; d.st[v] = ST_NARROW;
+  }
+  if (!grid_sync(ctl, nblocks, p.timeout_ns, ++where)) return;
+
+  int64_t it = 0;  // global iteration counter (identical in every block)
+  double cur_time = 0.0, phi_start = 0.0;
+  for (int32_t step = 0; step < p.n_steps; ++step) {
+    phi_start = cur_time;
+    cur_time += p.dt;
+    const double lower = phi_start - p.front_width;
+    int s = (int)(it % 3);
+    if (gtid == 0) {
+      for (int k = 0; k < 3; ++k) { ctl->n_narrow[k] = 0; ctl->n_frozen[k] = 0; ctl->n_marked[k] = 0; }
+    }
+    // sync_step2 (cuda_fim.cu:1752-1787): every copy of a mesh vertex takes
+    // the minimum over its copies; copies that were larger become narrow.
+    // (The reference indexes its interface table with the thread id instead
+    // of the loop index; that equals this whenever #vertices <= 256 *
+    // #submeshes, i.e. one vertex per thread.)
+    if (d.gptr) {
+      for (int64_t g = gtid; g < d.nG; g += nthreads) {
+        const int64_t k0 = d.gptr[g], k1 = d.gptr[g + 1];
+        double mn = FIM_INF;
+        for (int64_t k = k0; k < k1; ++k) {
+          const double v = __ldcg(d.phi + d.gcopy[k]);
+          if (v < mn) mn = v;
+        }
+        for (int64_t k = k0; k < k1; ++k) {
+          const int32_t c = d.gcopy[k];
+          if (mn < __ldcg(d.phi + c)) { d.phi[c] = mn; d.phi2[c] = mn; d.st[c] = ST_NARROW; }
+        }
+      }
+    }
+    if (!grid_sync(ctl, nblocks, p.timeout_ns, ++where)) return;
+    // update_states (cuda_fim.cu:1790-1845) -> narrow list of this window
+    for (int64_t v = gtid; v < d.nV; v += nthreads) {
+      uint8_t stv = d.st[v];
+      if (stv == ST_NEXT) { stv = ST_NARROW; d.st[v] = stv; }
+      else if (p.apd >= 0.0 && stv == ST_FROZEN) {
+        if (!(d.phi[v] + p.apd > cur_time)) d.st[v] = ST_TAIL;
+      } else if (p.apd >= 0.0 && stv == ST_TAIL) {
+        if (!(d.phi[v] + p.apd / 0.91 > cur_time)) {
+          d.phi[v] = FIM_INF; d.phi2[v] = FIM_INF; d.st[v] = ST_FAR;
+        }
+      }
+      if (stv == ST_NARROW) d.list[s][atomicAdd(&ctl->n_narrow[s], 1)] = (int32_t)v;
+    }
+    if (!grid_sync(ctl, nblocks, p.timeout_ns, ++where)) return;
+
+    int64_t it_window = 0;
+    for (;;) {
+      s = (int)(it % 3);
+      const int s1 = (int)((it + 1) % 3), s2 = (int)((it + 2) % 3);
+      const int32_t nn = ld_volatile_i32(&ctl->n_narrow[s]);
+      if (nn == 0) break;
+      if (p.max_iter > 0 && it_window >= p.max_iter) {
+        if (gtid == 0 && atomicCAS(&ctl->error, KERR_NONE, KERR_MAX_ITER) == KERR_NONE) ctl->error_where = where;
+        return;
+      }
+      const int32_t stamp = (int32_t)(it + 1);
+      const int32_t *lst = d.list[s];
+      int32_t *lnext = d.list[s1];
+      if (gtid == 0) { ctl->n_narrow[s2] = 0; ctl->n_frozen[s2] = 0; ctl->n_marked[s2] = 0; }
+
+      // P1 -- solve on elements + reduce per vertex (cuda_fim.cu:2102-2163)
+      for (int64_t i = w.gwarp; i < nn; i += w.nwarps) {
+        const int32_t v = lst[i];
+        const double best = warp_vertex_update(d, v, lower, w.lane, my_evals);
+        if (w.lane == 0) {
+          const double old = __ldcg(d.phi + v);
+          const double nw = (best < old) ? best : old;
+          d.phi2[v] = nw;
+          d.tst[v] = ST_FAR;
+          if (nw - phi_start > p.dt) {
+            d.st[v] = ST_NEXT;
+          } else if (fabs(old - nw) < (1e-6 * (1 + (old + nw) * .5))) {
+            d.tst[v] = ST_FROZEN;
+            d.lfrozen[atomicAdd(&ctl->n_frozen[s], 1)] = v;
+          }
+        }
+      }
+      my_updates += (gtid == 0) ? nn : 0;
+      if (!grid_sync(ctl, nblocks, p.timeout_ns, ++where)) return;
+
+      // P2 -- apply the narrow times; mark downwind neighbours of the
+      // vertices frozen now (cuda_fim.cu:2172-2205)
+      for (int64_t i = gtid; i < nn; i += nthreads) {
+        const int32_t v = lst[i];
+        d.phi[v] = __ldcg(d.phi2 + v);
+      }
+      const int32_t nf = ld_volatile_i32(&ctl->n_frozen[s]);
+      for (int64_t i = w.gwarp; i < nf; i += w.nwarps) {
+        const int32_t n = d.lfrozen[i];
+        const double pn = __ldcg(d.phi2 + n);
+        for (int64_t k = d.nptr[n] + w.lane; k < d.nptr[n + 1]; k += 32) {
+          const int32_t v = __ldg(d.nbr + k);
+          if (__ldcg(d.st + v) != ST_NARROW && pn < __ldcg(d.phi2 + v)) {
+            if (atomicExch(d.flag + v, stamp) != stamp) {
+              d.tst[v] = __ldcg(d.st + v);
+              d.st[v] = ST_NEIG;
+              d.lmarked[atomicAdd(&ctl->n_marked[s], 1)] = v;
+            }
+          }
+        }
+      }
+      if (!grid_sync(ctl, nblocks, p.timeout_ns, ++where)) return;
+
+      // P3 -- solve elements for neighbours + reduce (cuda_fim.cu:2215-2289)
+      const int32_t nm = ld_volatile_i32(&ctl->n_marked[s]);
+      for (int64_t i = w.gwarp; i < nm; i += w.nwarps) {
+        const int32_t v = d.lmarked[i];
+        const double best = warp_vertex_update(d, v, lower, w.lane, my_evals);
+        if (w.lane == 0) {
+          const double old = __ldcg(d.phi + v);
+          const double nw = (best < old) ? best : old;
+          d.phi2[v] = nw;
+          d.dec[i] = (nw < old) ? (uint8_t)ST_NARROW : __ldcg(d.tst + v);
+        }
+      }
+      my_updates += (gtid == 0) ? nm : 0;
+      if (!grid_sync(ctl, nblocks, p.timeout_ns, ++where)) return;
+
+      // P4 -- apply, update neighbour states, next narrow list (cuda_fim.cu:2291-2317)
+      for (int64_t i = gtid; i < nm; i += nthreads) {
+        const int32_t v = d.lmarked[i];
+        d.phi[v] = __ldcg(d.phi2 + v);
+        uint8_t sv = __ldcg(d.dec + i);
+        if (sv == ST_NARROW) {
+          if (__ldcg(d.tst + v) == ST_FROZEN) sv = ST_FROZEN;
+          else lnext[atomicAdd(&ctl->n_narrow[s1], 1)] = v;
+        }
+        d.st[v] = sv;
+      }
+      for (int64_t i = gtid; i < nn; i += nthreads) {
+        const int32_t v = lst[i];
+        if (__ldcg(d.flag + v) == stamp) continue;  // re-solved above
+        if (__ldcg(d.st + v) == ST_NARROW) {
+          if (__ldcg(d.tst + v) == ST_FROZEN) d.st[v] = ST_FROZEN;
+          else lnext[atomicAdd(&ctl->n_narrow[s1], 1)] = v;
+        }
+      }
+      ++it;
+      ++it_window;
+      if (!grid_sync(ctl, nblocks, p.timeout_ns, ++where)) return;
+    }
+  }
+
+  // local -> global gather (cuda_fim.cu:2466-2485): min time, max state
+  if (d.gptr) {
+    for (int64_t g = gtid; g < d.nG; g += nthreads) {
+      double mn = FIM_INF;
+      uint8_t mx = ST_FAR;
+      for (int64_t k = d.gptr[g]; k < d.gptr[g + 1]; ++k) {
+        const int32_t c = d.gcopy[k];
+        const double pc = __ldcg(d.phi + c);
+        const uint8_t sc = __ldcg(d.st + c);
+        if (pc < mn) mn = pc;
+        if (sc > mx) mx = sc;
+      }
+      d.phi_out[g] = mn;
+      d.st_out[g] = mx;
+    }
+  }
+
+  // statistics
+  __shared__ unsigned long long s_evals;
+  if (threadIdx.x == 0) s_evals = 0;
+  __syncthreads();
+  atomicAdd(&s_evals, (unsigned long long)my_evals);
+  __syncthreads();
+  if (threadIdx.x == 0) atomicAdd((unsigned long long *)&ctl->corner_evals, s_evals);
+  if (gtid == 0) {
+    ctl->iterations = it;
+    atomicAdd((unsigned long long *)&ctl->vertex_updates, (unsigned long long)my_updates);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// launch wrappers
+
+cudaError_t launch_metric(const int32_t *tslots, const int64_t *cidx, const double *xyz,
+                          const double *fib, const double *cf, const double *ct, int64_t nT,
+                          double *cgeo, cudaStream_t stream)
+{
+  if (nT <= 0) return cudaSuccess;
+  const int block = 256;
+  int64_t grid = (nT + block - 1) / block;
+  if (grid > 152 * 64) grid = 152 * 64;
+  fim_metric_kernel<<<(unsigned)grid, block, 0, stream>>>(tslots, cidx, xyz, fib, cf, ct, nT, cgeo);
+  return cudaGetLastError();
+}
+
+cudaError_t solve_grid_size(int device, int block, int *grid)
+{
+  int sms = 0, per_sm = 0;
+  cudaError_t e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  if (e != cudaSuccess) return e;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fim_solve_kernel, block, 0);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) per_sm = 1;
+  *grid = sms * per_sm;
+  return cudaSuccess;
+}
+
+cudaError_t launch_solve(const FimDev &d, const FimParams &p, int grid, int block, cudaStream_t stream)
+{
+  FimDev dd = d;
+  FimParams pp = p;
+  void *args[] = {&dd, &pp};
+  return cudaLaunchCooperativeKernel((const void *)fim_solve_kernel, dim3(grid), dim3(block), args, 0, stream);
+}
+
+__global__ void fim_copy_kernel(const double *__restrict__ src, double *__restrict__ dst, int64_t n)
+{
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    dst[i] = __ldcg(src + i);
+}
+
+cudaError_t launch_copy(const double *src, double *dst, int64_t n, cudaStream_t stream)
+{
+  if (n <= 0) return cudaSuccess;
+  int64_t grid = (n + 255) / 256;
+  if (grid > 152 * 32) grid = 152 * 32;
+  fim_copy_kernel<<<(unsigned)grid, 256, 0, stream>>>(src, dst, n);
+  return cudaGetLastError();
+}
+
+}  // namespace fimgb

@@ -1,0 +1,613 @@
+// fim_solver.cpp -- C ABI of the GB300 FIM solver (include/fim.h): solver
+// objects, mesh staging on the host, device buffers and launches.
+//
+// Host staging replaces the reference's CudaSolverFIM constructor
+// (src/eikonal/cuda_fim.cu:1218-1501): instead of per-submesh blobs with
+// in-blob pointers it builds flat device arrays --
+//   * the reference's vertex order inside every tet (extract_submeshes2,
+//     src/core/types.cpp:306-570: first appearance inside the tet's submesh,
+//     then ascending local id), which the local solver's result depends on;
+//   * one "corner" record per (vertex, tet): the other three vertices in the
+//     relabelled order of the reference's gray-code tables and the tet's six
+//     squared edge norms in that order (filled by the FP64 metric kernel);
+//   * the vertex neighbourhood (n2n incl. self, types.cpp:141-220).
+#include "fim_internal.h"
+#include "../../include/fim.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <new>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+using namespace fimgb;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+template <class T>
+struct DevBuf {
+  T *p = nullptr;
+  size_t n = 0;
+  cudaError_t alloc(size_t count)
+  {
+    release();
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+    if (e == cudaSuccess) n = count;
+    else p = nullptr;
+    return e;
+  }
+  void release()
+  {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  ~DevBuf() { release(); }
+};
+
+}  // namespace
+
+void fimgb::set_last_error(const char *msg) { g_last_error = msg; }
+
+struct fim_solver {
+  fim_opts opts{};
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  std::string err;
+  int grid = 0, block = 256;
+
+  // mesh (nL vertex copies: nL == nV with one submesh)
+  int64_t nV = 0, nT = 0, nC = 0, nL = 0;
+  int32_t n_submeshes = 1;
+  std::vector<uint8_t> in_tet;
+  std::vector<int64_t> h_gptr;
+  std::vector<int32_t> h_gcopy;
+  DevBuf<int64_t> gptr;
+  DevBuf<int32_t> gcopy;
+  DevBuf<double> phi_out;
+  DevBuf<uint8_t> st_out;
+  bool have_mesh = false, have_cond = false, have_stim = false, solved = false;
+  double front_width = 0.0;
+  DevBuf<double> xyz;
+  DevBuf<int32_t> tslots;
+  DevBuf<int64_t> cidx, cptr, nptr;
+  DevBuf<int4> cids;
+  DevBuf<double> cgeo;
+  DevBuf<int32_t> nbr;
+  DevBuf<double> fib, cf, ct;
+  // state
+  DevBuf<double> phi, phi2;
+  DevBuf<uint8_t> st, tst, dec;
+  DevBuf<int32_t> flag, list0, list1, list2, lfrozen, lmarked;
+  DevBuf<int32_t> seed_v;
+  DevBuf<double> seed_t;
+  int32_t nseed = 0;
+  DevBuf<FimCtl> ctl;
+  FimCtl last_ctl{};
+  fim_stats stats{};
+};
+
+static int set_err(fim_solver *s, int code, const char *fmt, ...)
+{
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  if (s) s->err = buf;
+  g_last_error = buf;
+  return code;
+}
+
+#define CUDA_TRY(s, call)                                                                     \
+  do {                                                                                        \
+    cudaError_t _e = (call);                                                                  \
+    if (_e != cudaSuccess) {                                                                  \
+      return set_err((s), _e == cudaErrorMemoryAllocation ? FIM_ERR_OUT_OF_MEMORY : FIM_ERR_CUDA, \
+                     "%s failed: %s (%s:%d)", #call, cudaGetErrorString(_e), __FILE__, __LINE__); \
+    }                                                                                         \
+  } while (0)
+
+extern "C" void fim_default_opts(fim_opts *o)
+{
+  if (!o) return;
+  std::memset(o, 0, sizeof(*o));
+  o->device = 0;
+  o->dt = std::numeric_limits<double>::infinity();
+  o->n_steps = 1;
+  o->front_width = -1.0;
+  o->apd = -1.0;
+  o->max_iterations = 0;
+  o->timeout_s = 10.0;
+  o->verbose = 0;
+}
+
+extern "C" const char *fim_last_error(const fim_solver *s)
+{
+  if (s) return s->err.c_str();
+  return g_last_error.c_str();
+}
+
+extern "C" int fim_create(const fim_opts *opts, fim_solver **out)
+{
+  if (!out) return set_err(nullptr, FIM_ERR_INVALID_ARGUMENT, "fim_create: out is NULL");
+  *out = nullptr;
+  fim_opts o;
+  if (opts) o = *opts;
+  else fim_default_opts(&o);
+  if (o.n_steps < 1) return set_err(nullptr, FIM_ERR_INVALID_ARGUMENT, "fim_create: n_steps must be >= 1");
+  if (!(o.dt > 0.0)) o.dt = std::numeric_limits<double>::infinity();
+  if (!(o.timeout_s > 0.0)) o.timeout_s = 10.0;
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev == 0)
+    return set_err(nullptr, FIM_ERR_NO_DEVICE, "fim_create: no CUDA device (%s)", cudaGetErrorString(e));
+  if (o.device < 0 || o.device >= ndev)
+    return set_err(nullptr, FIM_ERR_INVALID_ARGUMENT, "fim_create: device %d out of range [0,%d)", o.device, ndev);
+  fim_solver *s = new (std::nothrow) fim_solver();
+  if (!s) return set_err(nullptr, FIM_ERR_OUT_OF_MEMORY, "fim_create: out of host memory");
+  s->opts = o;
+  s->device = o.device;
+  if ((e = cudaSetDevice(s->device)) != cudaSuccess ||
+      (e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking)) != cudaSuccess ||
+      (e = cudaEventCreate(&s->ev0)) != cudaSuccess || (e = cudaEventCreate(&s->ev1)) != cudaSuccess ||
+      (e = solve_grid_size(s->device, s->block, &s->grid)) != cudaSuccess || (e = s->ctl.alloc(1)) != cudaSuccess) {
+    int rc = set_err(nullptr, FIM_ERR_CUDA, "fim_create: %s", cudaGetErrorString(e));
+    fim_destroy(s);
+    return rc;
+  }
+  int coop = 0;
+  cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, s->device);
+  if (!coop) {
+    fim_destroy(s);
+    return set_err(nullptr, FIM_ERR_NO_DEVICE, "fim_create: device does not support cooperative launch");
+  }
+  *out = s;
+  return FIM_OK;
+}
+
+extern "C" int fim_destroy(fim_solver *s)
+{
+  if (!s) return FIM_OK;
+  cudaSetDevice(s->device);
+  if (s->stream) cudaStreamSynchronize(s->stream);
+  if (s->ev0) cudaEventDestroy(s->ev0);
+  if (s->ev1) cudaEventDestroy(s->ev1);
+  if (s->stream) cudaStreamDestroy(s->stream);
+  s->stream = nullptr;
+  delete s;  // DevBuf destructors free device memory
+  return FIM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// mesh staging
+
+namespace {
+
+// The reference's slot order of every tet: aggregates numbered by first
+// appearance of their tag, local vertex ids by first appearance while
+// walking the aggregate's tets in increasing tet index with each tet's
+// global ids ascending, then each tet's local ids ascending
+// (types.cpp:63-67, 331-345, 383-398, 473).
+//   slots  -- 4*nT mesh vertex ids in slot order (for the metric)
+//   cslots -- 4*nT vertex-copy ids in slot order (for the corners)
+//   gptr/gcopy -- copies of every mesh vertex (left empty with one submesh,
+//                 where copy == vertex)
+struct Staging {
+  std::vector<int32_t> slots, cslots;
+  int64_t n_copies = 0;
+  int32_t n_submeshes = 1;
+  std::vector<int64_t> gptr;
+  std::vector<int32_t> gcopy;
+};
+
+void reference_slots(int64_t nV, int64_t nT, const int64_t *tets, const int32_t *atags, Staging &S)
+{
+  S.slots.resize(4 * nT);
+  S.cslots.resize(4 * nT);
+  std::vector<int32_t> agg(nT, 0);
+  int32_t nagg = 1;
+  if (atags) {
+    std::unordered_map<int32_t, int32_t> t2a;
+    nagg = 0;
+    for (int64_t e = 0; e < nT; ++e) {
+      auto it = t2a.find(atags[e]);
+      if (it == t2a.end()) it = t2a.emplace(atags[e], nagg++).first;
+      agg[e] = it->second;
+    }
+  }
+  S.n_submeshes = nagg;
+  // tets grouped by aggregate, increasing index inside each group
+  std::vector<int64_t> aptr(nagg + 1, 0), order(nT);
+  for (int64_t e = 0; e < nT; ++e) aptr[agg[e] + 1]++;
+  for (int32_t a = 0; a < nagg; ++a) aptr[a + 1] += aptr[a];
+  {
+    std::vector<int64_t> fill(aptr.begin(), aptr.end() - 1);
+    for (int64_t e = 0; e < nT; ++e) order[fill[agg[e]]++] = e;
+  }
+  std::vector<int64_t> rank(nV, -1);  // first-appearance rank inside the current aggregate
+  std::vector<int32_t> touched;
+  std::vector<int32_t> copy_owner;    // copy -> mesh vertex (several submeshes)
+  int64_t base = 0;
+  for (int32_t a = 0; a < nagg; ++a) {
+    int64_t next = 0;
+    for (int64_t k = aptr[a]; k < aptr[a + 1]; ++k) {
+      const int64_t e = order[k];
+      int64_t g[4] = {tets[4 * e], tets[4 * e + 1], tets[4 * e + 2], tets[4 * e + 3]};
+      std::sort(g, g + 4);
+      for (int j = 0; j < 4; ++j)
+        if (rank[g[j]] < 0) {
+          rank[g[j]] = next++;
+          touched.push_back((int32_t)g[j]);
+          if (nagg > 1) copy_owner.push_back((int32_t)g[j]);
+        }
+      std::sort(g, g + 4, [&](int64_t x, int64_t y) { return rank[x] < rank[y]; });
+      for (int j = 0; j < 4; ++j) {
+        S.slots[4 * e + j] = (int32_t)g[j];
+        S.cslots[4 * e + j] = nagg > 1 ? (int32_t)(base + rank[g[j]]) : (int32_t)g[j];
+      }
+    }
+    base += next;
+    for (int32_t v : touched) rank[v] = -1;
+    touched.clear();
+  }
+  if (nagg > 1) {
+    S.n_copies = base;
+    S.gptr.assign(nV + 1, 0);
+    for (int32_t g : copy_owner) S.gptr[g + 1]++;
+    for (int64_t v = 0; v < nV; ++v) S.gptr[v + 1] += S.gptr[v];
+    S.gcopy.resize(base);
+    std::vector<int64_t> fill(S.gptr.begin(), S.gptr.end() - 1);
+    for (int64_t c = 0; c < base; ++c) S.gcopy[fill[copy_owner[c]]++] = (int32_t)c;
+  } else {
+    S.n_copies = nV;
+  }
+}
+
+}  // namespace
+
+extern "C" int fim_set_mesh(fim_solver *s, int64_t nV, const double *xyz, int64_t nT, const int64_t *tets,
+                            const int32_t *atags)
+{
+  if (!s) return set_err(nullptr, FIM_ERR_INVALID_ARGUMENT, "fim_set_mesh: solver is NULL");
+  if (nV <= 0 || nT <= 0 || !xyz || !tets)
+    return set_err(s, FIM_ERR_INVALID_ARGUMENT, "fim_set_mesh: empty mesh or NULL array");
+  if (nV >= (int64_t)INT32_MAX || 4 * nT >= (int64_t)INT32_MAX)
+    return set_err(s, FIM_ERR_INVALID_ARGUMENT, "fim_set_mesh: mesh too large (%lld vertices, %lld tets)",
+                   (long long)nV, (long long)nT);
+  for (int64_t i = 0; i < 4 * nT; ++i)
+    if (tets[i] < 0 || tets[i] >= nV)
+      return set_err(s, FIM_ERR_INVALID_ARGUMENT, "fim_set_mesh: tet %lld has vertex %lld outside [0,%lld)",
+                     (long long)(i / 4), (long long)tets[i], (long long)nV);
+  for (int64_t e = 0; e < nT; ++e) {
+    const int64_t *t = tets + 4 * e;
+    if (t[0] == t[1] || t[0] == t[2] || t[0] == t[3] || t[1] == t[2] || t[1] == t[3] || t[2] == t[3])
+      return set_err(s, FIM_ERR_INVALID_ARGUMENT, "fim_set_mesh: tet %lld repeats a vertex", (long long)e);
+  }
+  for (int64_t i = 0; i < 3 * nV; ++i)
+    if (!std::isfinite(xyz[i]))
+      return set_err(s, FIM_ERR_INVALID_ARGUMENT, "fim_set_mesh: coordinate %lld is not finite", (long long)i);
+
+  Staging S;
+  reference_slots(nV, nT, tets, atags, S);
+  const std::vector<int32_t> &slots = S.slots;
+  const int64_t nL = S.n_copies;
+
+  // corners of every vertex copy, in increasing tet index
+  const int64_t nC = 4 * nT;
+  std::vector<int64_t> cptr(nL + 1, 0), cidx(nC);
+  for (int64_t i = 0; i < nC; ++i) cptr[S.cslots[i] + 1]++;
+  for (int64_t v = 0; v < nL; ++v) cptr[v + 1] += cptr[v];
+  std::vector<int4> cids(nC);
+  {
+    std::vector<int64_t> fill(cptr.begin(), cptr.end() - 1);
+    for (int64_t e = 0; e < nT; ++e)
+      for (int t = 0; t < 4; ++t) {
+        const int32_t v = S.cslots[4 * e + t];
+        const int64_t c = fill[v]++;
+        cidx[4 * e + t] = c;
+        cids[c] = make_int4(S.cslots[4 * e + ((t + 1) & 3)], S.cslots[4 * e + ((t + 2) & 3)],
+                            S.cslots[4 * e + ((t + 3) & 3)], (int)e);
+      }
+  }
+  // neighbourhood of every copy incl. itself (sorted), two passes
+  std::vector<int64_t> nptr(nL + 1, 0);
+  std::vector<int32_t> nbr;
+  {
+    std::vector<int32_t> cnt(nL);
+#pragma omp parallel
+    {
+      std::vector<int32_t> buf;
+#pragma omp for schedule(static)
+      for (int64_t v = 0; v < nL; ++v) {
+        buf.clear();
+        buf.push_back((int32_t)v);
+        for (int64_t c = cptr[v]; c < cptr[v + 1]; ++c) {
+          buf.push_back(cids[c].x); buf.push_back(cids[c].y); buf.push_back(cids[c].z);
+        }
+        std::sort(buf.begin(), buf.end());
+        cnt[v] = (int32_t)(std::unique(buf.begin(), buf.end()) - buf.begin());
+      }
+    }
+    for (int64_t v = 0; v < nL; ++v) nptr[v + 1] = nptr[v] + cnt[v];
+    nbr.resize(nptr[nL]);
+#pragma omp parallel
+    {
+      std::vector<int32_t> buf;
+#pragma omp for schedule(static)
+      for (int64_t v = 0; v < nL; ++v) {
+        buf.clear();
+        buf.push_back((int32_t)v);
+        for (int64_t c = cptr[v]; c < cptr[v + 1]; ++c) {
+          buf.push_back(cids[c].x); buf.push_back(cids[c].y); buf.push_back(cids[c].z);
+        }
+        std::sort(buf.begin(), buf.end());
+        const int64_t m = std::unique(buf.begin(), buf.end()) - buf.begin();
+        std::copy(buf.begin(), buf.begin() + m, nbr.begin() + nptr[v]);
+      }
+    }
+  }
+  // vertices in at least one tet (seeds elsewhere are dropped, as the
+  // reference seeds through submeshes only)
+  std::vector<uint8_t> in_tet(nV, 0);
+  for (int64_t i = 0; i < nC; ++i) in_tet[slots[i]] = 1;
+  // reference front width: 1.01 * longest edge / 0.6 (compute_dwf, cuda_fim.h:1536-1576)
+  double maxe2 = 0.0;
+  for (int64_t e = 0; e < nT; ++e)
+    for (int i = 0; i < 4; ++i)
+      for (int j = i + 1; j < 4; ++j) {
+        const int64_t a = tets[4 * e + i], b = tets[4 * e + j];
+        const double dx = xyz[3 * b] - xyz[3 * a], dy = xyz[3 * b + 1] - xyz[3 * a + 1], dz = xyz[3 * b + 2] - xyz[3 * a + 2];
+        const double l = dx * dx + dy * dy + dz * dz;
+        if (l > maxe2) maxe2 = l;
+      }
+  s->front_width = 1.01 * std::sqrt(maxe2) / 0.6;
+
+  CUDA_TRY(s, cudaSetDevice(s->device));
+  s->have_mesh = s->have_cond = s->have_stim = s->solved = false;
+  s->nV = nV; s->nT = nT; s->nC = nC; s->nL = nL;
+  s->n_submeshes = S.n_submeshes;
+  s->in_tet.swap(in_tet);
+  s->h_gptr.swap(S.gptr);
+  s->h_gcopy.swap(S.gcopy);
+  const bool multi = S.n_submeshes > 1;
+  CUDA_TRY(s, s->xyz.alloc(3 * nV));
+  CUDA_TRY(s, s->tslots.alloc(4 * nT));
+  CUDA_TRY(s, s->cidx.alloc(nC));
+  CUDA_TRY(s, s->cptr.alloc(nL + 1));
+  CUDA_TRY(s, s->cids.alloc(nC));
+  CUDA_TRY(s, s->cgeo.alloc(10 * nC));
+  CUDA_TRY(s, s->nptr.alloc(nL + 1));
+  CUDA_TRY(s, s->nbr.alloc(nbr.size()));
+  CUDA_TRY(s, s->fib.alloc(3 * nT));
+  CUDA_TRY(s, s->cf.alloc(nT));
+  CUDA_TRY(s, s->ct.alloc(nT));
+  CUDA_TRY(s, s->phi.alloc(nL));
+  CUDA_TRY(s, s->phi2.alloc(nL));
+  CUDA_TRY(s, s->st.alloc(nL));
+  CUDA_TRY(s, s->tst.alloc(nL));
+  CUDA_TRY(s, s->dec.alloc(nL));
+  CUDA_TRY(s, s->flag.alloc(nL));
+  CUDA_TRY(s, s->list0.alloc(nL));
+  CUDA_TRY(s, s->list1.alloc(nL));
+  CUDA_TRY(s, s->list2.alloc(nL));
+  CUDA_TRY(s, s->lfrozen.alloc(nL));
+  CUDA_TRY(s, s->lmarked.alloc(nL));
+  if (multi) {
+    CUDA_TRY(s, s->gptr.alloc(nV + 1));
+    CUDA_TRY(s, s->gcopy.alloc(nL));
+    CUDA_TRY(s, s->phi_out.alloc(nV));
+    CUDA_TRY(s, s->st_out.alloc(nV));
+  } else {
+    s->gptr.release(); s->gcopy.release(); s->phi_out.release(); s->st_out.release();
+  }
+  cudaStream_t st = s->stream;
+  CUDA_TRY(s, cudaMemcpyAsync(s->xyz.p, xyz, sizeof(double) * 3 * nV, cudaMemcpyHostToDevice, st));
+  CUDA_TRY(s, cudaMemcpyAsync(s->tslots.p, slots.data(), sizeof(int32_t) * 4 * nT, cudaMemcpyHostToDevice, st));
+  CUDA_TRY(s, cudaMemcpyAsync(s->cidx.p, cidx.data(), sizeof(int64_t) * nC, cudaMemcpyHostToDevice, st));
+  CUDA_TRY(s, cudaMemcpyAsync(s->cptr.p, cptr.data(), sizeof(int64_t) * (nL + 1), cudaMemcpyHostToDevice, st));
+  CUDA_TRY(s, cudaMemcpyAsync(s->cids.p, cids.data(), sizeof(int4) * nC, cudaMemcpyHostToDevice, st));
+  CUDA_TRY(s, cudaMemcpyAsync(s->nptr.p, nptr.data(), sizeof(int64_t) * (nL + 1), cudaMemcpyHostToDevice, st));
+  CUDA_TRY(s, cudaMemcpyAsync(s->nbr.p, nbr.data(), sizeof(int32_t) * nbr.size(), cudaMemcpyHostToDevice, st));
+  if (multi) {
+    CUDA_TRY(s, cudaMemcpyAsync(s->gptr.p, s->h_gptr.data(), sizeof(int64_t) * (nV + 1), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(s, cudaMemcpyAsync(s->gcopy.p, s->h_gcopy.data(), sizeof(int32_t) * nL, cudaMemcpyHostToDevice, st));
+  }
+  CUDA_TRY(s, cudaStreamSynchronize(st));
+  s->stats.n_corners = nC;
+  s->have_mesh = true;
+  return FIM_OK;
+}
+
+static int run_metric(fim_solver *s)
+{
+  CUDA_TRY(s, cudaEventRecord(s->ev0, s->stream));
+  CUDA_TRY(s, launch_metric(s->tslots.p, s->cidx.p, s->xyz.p, s->fib.p, s->cf.p, s->ct.p, s->nT, s->cgeo.p,
+                            s->stream));
+  CUDA_TRY(s, cudaEventRecord(s->ev1, s->stream));
+  CUDA_TRY(s, cudaEventSynchronize(s->ev1));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, s->ev0, s->ev1);
+  s->stats.metric_ms = ms;
+  s->have_cond = true;
+  s->solved = false;
+  return FIM_OK;
+}
+
+extern "C" int fim_set_conduction(fim_solver *s, const double *fib, const double *cf, const double *ct)
+{
+  if (!s) return set_err(nullptr, FIM_ERR_INVALID_ARGUMENT, "fim_set_conduction: solver is NULL");
+  if (!s->have_mesh) return set_err(s, FIM_ERR_NOT_READY, "fim_set_conduction: no mesh");
+  if (!fib || !cf || !ct) return set_err(s, FIM_ERR_INVALID_ARGUMENT, "fim_set_conduction: NULL array");
+  for (int64_t e = 0; e < s->nT; ++e) {
+    if (!(cf[e] > 0.0) || !(ct[e] > 0.0) || !std::isfinite(cf[e]) || !std::isfinite(ct[e]))
+      return set_err(s, FIM_ERR_INVALID_ARGUMENT, "fim_set_conduction: tet %lld has speed cf=%g ct=%g",
+                     (long long)e, cf[e], ct[e]);
+    if (!std::isfinite(fib[3 * e]) || !std::isfinite(fib[3 * e + 1]) || !std::isfinite(fib[3 * e + 2]))
+      return set_err(s, FIM_ERR_INVALID_ARGUMENT, "fim_set_conduction: tet %lld has a non-finite fibre",
+                     (long long)e);
+  }
+  CUDA_TRY(s, cudaSetDevice(s->device));
+  CUDA_TRY(s, cudaMemcpyAsync(s->fib.p, fib, sizeof(double) * 3 * s->nT, cudaMemcpyHostToDevice, s->stream));
+  CUDA_TRY(s, cudaMemcpyAsync(s->cf.p, cf, sizeof(double) * s->nT, cudaMemcpyHostToDevice, s->stream));
+  CUDA_TRY(s, cudaMemcpyAsync(s->ct.p, ct, sizeof(double) * s->nT, cudaMemcpyHostToDevice, s->stream));
+  return run_metric(s);
+}
+
+extern "C" int fim_set_conduction_device(fim_solver *s, const double *d_fib, const double *d_cf, const double *d_ct)
+{
+  if (!s) return set_err(nullptr, FIM_ERR_INVALID_ARGUMENT, "fim_set_conduction_device: solver is NULL");
+  if (!s->have_mesh) return set_err(s, FIM_ERR_NOT_READY, "fim_set_conduction_device: no mesh");
+  if (!d_fib || !d_cf || !d_ct) return set_err(s, FIM_ERR_INVALID_ARGUMENT, "fim_set_conduction_device: NULL array");
+  CUDA_TRY(s, cudaSetDevice(s->device));
+  CUDA_TRY(s, cudaMemcpyAsync(s->fib.p, d_fib, sizeof(double) * 3 * s->nT, cudaMemcpyDeviceToDevice, s->stream));
+  CUDA_TRY(s, cudaMemcpyAsync(s->cf.p, d_cf, sizeof(double) * s->nT, cudaMemcpyDeviceToDevice, s->stream));
+  CUDA_TRY(s, cudaMemcpyAsync(s->ct.p, d_ct, sizeof(double) * s->nT, cudaMemcpyDeviceToDevice, s->stream));
+  return run_metric(s);
+}
+
+extern "C" int fim_set_stimuli(fim_solver *s, int64_t n, const int64_t *vertices, const double *t0)
+{
+  if (!s) return set_err(nullptr, FIM_ERR_INVALID_ARGUMENT, "fim_set_stimuli: solver is NULL");
+  if (!s->have_mesh) return set_err(s, FIM_ERR_NOT_READY, "fim_set_stimuli: no mesh");
+  if (n < 0 || (n > 0 && (!vertices || !t0)))
+    return set_err(s, FIM_ERR_INVALID_ARGUMENT, "fim_set_stimuli: bad count or NULL array");
+  // one entry per vertex: the earliest start time
+  std::unordered_map<int64_t, double> first;
+  for (int64_t i = 0; i < n; ++i) {
+    if (vertices[i] < 0 || vertices[i] >= s->nV)
+      return set_err(s, FIM_ERR_INVALID_ARGUMENT, "fim_set_stimuli: vertex %lld outside [0,%lld)",
+                     (long long)vertices[i], (long long)s->nV);
+    if (!std::isfinite(t0[i]))
+      return set_err(s, FIM_ERR_INVALID_ARGUMENT, "fim_set_stimuli: start time %lld is not finite", (long long)i);
+    auto it = first.find(vertices[i]);
+    if (it == first.end()) first.emplace(vertices[i], t0[i]);
+    else if (t0[i] < it->second) it->second = t0[i];
+  }
+  // every copy of a stimulated vertex is seeded (update_events_gpu seeds
+  // through the submeshes holding the vertex, cuda_fim.cu:1422-1487)
+  std::vector<int32_t> v;
+  std::vector<double> t;
+  v.reserve(first.size());
+  t.reserve(first.size());
+  for (int64_t i = 0; i < n; ++i) {
+    auto it = first.find(vertices[i]);
+    if (it == first.end()) continue;
+    const int64_t g = it->first;
+    if (s->in_tet[g]) {
+      if (s->h_gptr.empty()) { v.push_back((int32_t)g); t.push_back(it->second); }
+      else
+        for (int64_t k = s->h_gptr[g]; k < s->h_gptr[g + 1]; ++k) { v.push_back(s->h_gcopy[k]); t.push_back(it->second); }
+    }
+    first.erase(it);
+  }
+  CUDA_TRY(s, cudaSetDevice(s->device));
+  CUDA_TRY(s, s->seed_v.alloc(v.size()));
+  CUDA_TRY(s, s->seed_t.alloc(t.size()));
+  if (!v.empty()) {
+    CUDA_TRY(s, cudaMemcpyAsync(s->seed_v.p, v.data(), sizeof(int32_t) * v.size(), cudaMemcpyHostToDevice, s->stream));
+    CUDA_TRY(s, cudaMemcpyAsync(s->seed_t.p, t.data(), sizeof(double) * t.size(), cudaMemcpyHostToDevice, s->stream));
+    CUDA_TRY(s, cudaStreamSynchronize(s->stream));
+  }
+  s->nseed = (int32_t)v.size();
+  s->have_stim = true;
+  s->solved = false;
+  return FIM_OK;
+}
+
+extern "C" int fim_solve(fim_solver *s, void *stream)
+{
+  if (!s) return set_err(nullptr, FIM_ERR_INVALID_ARGUMENT, "fim_solve: solver is NULL");
+  if (!s->have_mesh || !s->have_cond || !s->have_stim)
+    return set_err(s, FIM_ERR_NOT_READY, "fim_solve: mesh, conduction and stimuli must be set first");
+  CUDA_TRY(s, cudaSetDevice(s->device));
+  cudaStream_t st = stream ? (cudaStream_t)stream : s->stream;
+  FimDev d{};
+  d.nV = (int32_t)s->nL; d.nG = (int32_t)s->nV; d.nT = s->nT; d.nC = s->nC;
+  d.gptr = s->gptr.p; d.gcopy = s->gcopy.p; d.phi_out = s->phi_out.p; d.st_out = s->st_out.p;
+  d.cptr = s->cptr.p; d.cids = s->cids.p; d.cgeo = s->cgeo.p; d.nptr = s->nptr.p; d.nbr = s->nbr.p;
+  d.phi = s->phi.p; d.phi2 = s->phi2.p; d.st = s->st.p; d.tst = s->tst.p; d.flag = s->flag.p;
+  d.list[0] = s->list0.p; d.list[1] = s->list1.p; d.list[2] = s->list2.p;
+  d.lfrozen = s->lfrozen.p; d.lmarked = s->lmarked.p; d.dec = s->dec.p;
+  d.seed_v = s->seed_v.p; d.seed_t = s->seed_t.p; d.nseed = s->nseed;
+  d.ctl = s->ctl.p;
+  FimParams p{};
+  p.dt = s->opts.dt;
+  p.n_steps = s->opts.n_steps;
+  p.front_width = s->opts.front_width >= 0.0 ? s->opts.front_width : s->front_width;
+  p.apd = s->opts.apd;
+  p.max_iter = s->opts.max_iterations > 0 ? s->opts.max_iterations : 10000000;
+  p.timeout_ns = (uint64_t)(s->opts.timeout_s * 1e9);
+  CUDA_TRY(s, cudaMemsetAsync(s->ctl.p, 0, sizeof(FimCtl), st));
+  CUDA_TRY(s, cudaEventRecord(s->ev0, st));
+  CUDA_TRY(s, launch_solve(d, p, s->grid, s->block, st));
+  CUDA_TRY(s, cudaEventRecord(s->ev1, st));
+  CUDA_TRY(s, cudaMemcpyAsync(&s->last_ctl, s->ctl.p, sizeof(FimCtl), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(s, cudaStreamSynchronize(st));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, s->ev0, s->ev1);
+  s->stats.solve_ms = ms;
+  s->stats.iterations = s->last_ctl.iterations;
+  s->stats.vertex_updates = s->last_ctl.vertex_updates;
+  s->stats.corner_evals = s->last_ctl.corner_evals;
+  s->stats.grid_blocks = s->grid;
+  s->stats.block_threads = s->block;
+  if (s->last_ctl.error == KERR_TIMEOUT)
+    return set_err(s, FIM_ERR_TIMEOUT, "fim_solve: a grid barrier wait exceeded %.3f s (phase %d)",
+                   s->opts.timeout_s, s->last_ctl.error_where);
+  if (s->last_ctl.error == KERR_MAX_ITER)
+    return set_err(s, FIM_ERR_MAX_ITERATIONS, "fim_solve: iteration cap %lld reached in a window",
+                   (long long)p.max_iter);
+  s->solved = true;
+  return FIM_OK;
+}
+
+extern "C" int fim_get_times(fim_solver *s, double *phi, int32_t *state)
+{
+  if (!s) return set_err(nullptr, FIM_ERR_INVALID_ARGUMENT, "fim_get_times: solver is NULL");
+  if (!s->solved) return set_err(s, FIM_ERR_NOT_READY, "fim_get_times: no finished solve");
+  CUDA_TRY(s, cudaSetDevice(s->device));
+  const double *dphi = s->phi_out.p ? s->phi_out.p : s->phi.p;
+  const uint8_t *dst = s->st_out.p ? s->st_out.p : s->st.p;
+  if (phi) CUDA_TRY(s, cudaMemcpyAsync(phi, dphi, sizeof(double) * s->nV, cudaMemcpyDeviceToHost, s->stream));
+  std::vector<uint8_t> st8;
+  if (state) {
+    st8.resize(s->nV);
+    CUDA_TRY(s, cudaMemcpyAsync(st8.data(), dst, s->nV, cudaMemcpyDeviceToHost, s->stream));
+  }
+  CUDA_TRY(s, cudaStreamSynchronize(s->stream));
+  if (state)
+    for (int64_t v = 0; v < s->nV; ++v) state[v] = st8[v];
+  return FIM_OK;
+}
+
+extern "C" int fim_get_times_device(fim_solver *s, double *d_phi)
+{
+  if (!s) return set_err(nullptr, FIM_ERR_INVALID_ARGUMENT, "fim_get_times_device: solver is NULL");
+  if (!s->solved) return set_err(s, FIM_ERR_NOT_READY, "fim_get_times_device: no finished solve");
+  if (!d_phi) return set_err(s, FIM_ERR_INVALID_ARGUMENT, "fim_get_times_device: NULL pointer");
+  CUDA_TRY(s, cudaSetDevice(s->device));
+  CUDA_TRY(s, launch_copy(s->phi_out.p ? s->phi_out.p : s->phi.p, d_phi, s->nV, s->stream));
+  CUDA_TRY(s, cudaStreamSynchronize(s->stream));
+  return FIM_OK;
+}
+
+extern "C" int fim_get_stats(const fim_solver *s, fim_stats *out)
+{
+  if (!s || !out) return set_err(nullptr, FIM_ERR_INVALID_ARGUMENT, "fim_get_stats: NULL argument");
+  *out = s->stats;
+  return FIM_OK;
+}

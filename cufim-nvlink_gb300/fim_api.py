@@ -1,0 +1,228 @@
+"""Python front end of the GB300 FIM solver: a ctypes binding of the C ABI in
+include/fim.h (libfim_gb300.so, built in-tree by build.py).
+
+This module is glue for tests, benchmarks and scripting; all arithmetic runs
+in the library's CUDA kernels.  Loading fails loudly when the library is
+missing -- there is no fallback path.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libfim_gb300.so")
+INF = np.finfo(np.float64).max  # the reference's INF (DBL_MAX) for unreached vertices
+
+FIM_OK = 0
+STATUS = {0: "FIM_OK", 1: "FIM_ERR_INVALID_ARGUMENT", 2: "FIM_ERR_CUDA", 3: "FIM_ERR_NOT_READY",
+          4: "FIM_ERR_TIMEOUT", 5: "FIM_ERR_MAX_ITERATIONS", 6: "FIM_ERR_IO", 7: "FIM_ERR_OUT_OF_MEMORY",
+          8: "FIM_ERR_NO_DEVICE"}
+FAR, NEIG, NARROW, NEXT, FROZEN, TAIL = range(6)
+
+# every symbol declared in include/fim.h
+EXPORTS = ["fim_default_opts", "fim_create", "fim_destroy", "fim_last_error", "fim_set_mesh",
+           "fim_set_conduction", "fim_set_conduction_device", "fim_set_stimuli", "fim_solve",
+           "fim_get_times", "fim_get_times_device", "fim_get_stats", "fim_vtk_read", "fim_vtk_write",
+           "fim_read_tags", "fim_load_plan"]
+
+
+class FimOpts(C.Structure):
+    _fields_ = [("device", C.c_int), ("dt", C.c_double), ("n_steps", C.c_int), ("front_width", C.c_double),
+                ("apd", C.c_double), ("max_iterations", C.c_int64), ("timeout_s", C.c_double),
+                ("verbose", C.c_int)]
+
+
+class FimStats(C.Structure):
+    _fields_ = [("iterations", C.c_int64), ("vertex_updates", C.c_int64), ("corner_evals", C.c_int64),
+                ("solve_ms", C.c_double), ("metric_ms", C.c_double), ("n_corners", C.c_int64),
+                ("grid_blocks", C.c_int), ("block_threads", C.c_int)]
+
+
+class FimPlanInfo(C.Structure):
+    _fields_ = [("dt", C.c_double), ("n_steps", C.c_int64), ("n_events", C.c_int64),
+                ("n_stim_vertices", C.c_int64), ("cv", C.c_double * 3), ("tstart", C.c_double),
+                ("has_cv", C.c_int)]
+
+
+class FimError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{STATUS.get(code, code)}: {msg}")
+        self.code = code
+
+
+_lib = None
+
+
+def lib():
+    """Load libfim_gb300.so (raises if it was not built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise FimError(8, f"{LIB_PATH} not built; run cufim-nvlink_gb300/build.py")
+        L = C.CDLL(LIB_PATH)
+        P, d, i32, i64, vp = C.POINTER, C.c_double, C.c_int32, C.c_int64, C.c_void_p
+        L.fim_default_opts.argtypes = [P(FimOpts)]
+        L.fim_default_opts.restype = None
+        L.fim_create.argtypes = [P(FimOpts), P(vp)]
+        L.fim_destroy.argtypes = [vp]
+        L.fim_last_error.argtypes = [vp]
+        L.fim_last_error.restype = C.c_char_p
+        L.fim_set_mesh.argtypes = [vp, i64, P(d), i64, P(i64), P(i32)]
+        L.fim_set_conduction.argtypes = [vp, P(d), P(d), P(d)]
+        L.fim_set_conduction_device.argtypes = [vp, vp, vp, vp]
+        L.fim_set_stimuli.argtypes = [vp, i64, P(i64), P(d)]
+        L.fim_solve.argtypes = [vp, vp]
+        L.fim_get_times.argtypes = [vp, P(d), P(i32)]
+        L.fim_get_times_device.argtypes = [vp, vp]
+        L.fim_get_stats.argtypes = [vp, P(FimStats)]
+        L.fim_vtk_read.argtypes = [C.c_char_p, P(i64), P(i64), P(d), P(i64), P(i32)]
+        L.fim_vtk_write.argtypes = [C.c_char_p, i64, i64, P(d), P(i64), P(i32), P(d), P(d)]
+        L.fim_read_tags.argtypes = [C.c_char_p, P(i64), P(i32)]
+        L.fim_load_plan.argtypes = [C.c_char_p, C.c_char_p, P(FimPlanInfo), P(i64)]
+        for name in EXPORTS:
+            getattr(L, name)
+        _lib = L
+    return _lib
+
+
+def _ptr(a, t):
+    return None if a is None else a.ctypes.data_as(C.POINTER(t))
+
+
+def _check(rc, handle=None):
+    if rc != FIM_OK:
+        msg = lib().fim_last_error(handle)
+        raise FimError(rc, msg.decode() if msg else "")
+
+
+def default_opts(**kw):
+    o = FimOpts()
+    lib().fim_default_opts(C.byref(o))
+    for k, v in kw.items():
+        setattr(o, k, v)
+    return o
+
+
+class Solver:
+    """One GPU solver object (a fim_solver handle)."""
+
+    def __init__(self, **opts):
+        self.h = C.c_void_p()
+        o = default_opts(**opts)
+        _check(lib().fim_create(C.byref(o), C.byref(self.h)))
+        self.nV = 0
+        self.nT = 0
+
+    def close(self):
+        if self.h:
+            lib().fim_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def set_mesh(self, xyz, tets, atags=None):
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+        tets = np.ascontiguousarray(tets, dtype=np.int64)
+        at = None if atags is None else np.ascontiguousarray(atags, dtype=np.int32)
+        self.nV = xyz.shape[0]
+        self.nT = tets.shape[0]
+        _check(lib().fim_set_mesh(self.h, self.nV, _ptr(xyz, C.c_double), self.nT, _ptr(tets, C.c_int64),
+                                  _ptr(at, C.c_int32)), self.h)
+
+    def set_conduction(self, fib, cf, ct):
+        fib = np.ascontiguousarray(fib, dtype=np.float64)
+        cf = np.ascontiguousarray(cf, dtype=np.float64)
+        ct = np.ascontiguousarray(ct, dtype=np.float64)
+        _check(lib().fim_set_conduction(self.h, _ptr(fib, C.c_double), _ptr(cf, C.c_double),
+                                        _ptr(ct, C.c_double)), self.h)
+
+    def set_conduction_device(self, fib_ptr, cf_ptr, ct_ptr):
+        _check(lib().fim_set_conduction_device(self.h, C.c_void_p(fib_ptr), C.c_void_p(cf_ptr),
+                                               C.c_void_p(ct_ptr)), self.h)
+
+    def set_stimuli(self, vertices, t0):
+        v = np.ascontiguousarray(vertices, dtype=np.int64)
+        t = np.ascontiguousarray(t0, dtype=np.float64)
+        _check(lib().fim_set_stimuli(self.h, v.shape[0], _ptr(v, C.c_int64), _ptr(t, C.c_double)), self.h)
+
+    def solve(self, stream=None):
+        _check(lib().fim_solve(self.h, C.c_void_p(stream) if stream else None), self.h)
+
+    def times(self, with_state=True):
+        phi = np.empty(self.nV, dtype=np.float64)
+        st = np.empty(self.nV, dtype=np.int32) if with_state else None
+        _check(lib().fim_get_times(self.h, _ptr(phi, C.c_double), _ptr(st, C.c_int32)), self.h)
+        return (phi, st) if with_state else phi
+
+    def times_device(self, dptr):
+        _check(lib().fim_get_times_device(self.h, C.c_void_p(dptr)), self.h)
+
+    def stats(self):
+        s = FimStats()
+        _check(lib().fim_get_stats(self.h, C.byref(s)), self.h)
+        return {k: getattr(s, k) for k, _ in FimStats._fields_}
+
+
+def solve_case(case, atags=None, **opts):
+    """Convenience: one solve of a case dict (xyz, tets, fib, cf, ct, seed_v, seed_t)."""
+    with Solver(**opts) as s:
+        s.set_mesh(case["xyz"], case["tets"], atags)
+        s.set_conduction(case["fib"], case["cf"], case["ct"])
+        s.set_stimuli(case["seed_v"], case["seed_t"])
+        s.solve()
+        phi, st = s.times()
+        return phi, st, s.stats()
+
+
+# ---------------------------------------------------------------------------
+# reference-compatible files
+
+def vtk_read(path):
+    nV, nT = C.c_int64(), C.c_int64()
+    _check(lib().fim_vtk_read(path.encode(), C.byref(nV), C.byref(nT), None, None, None))
+    xyz = np.empty((nV.value, 3), dtype=np.float64)
+    tets = np.empty((nT.value, 4), dtype=np.int64)
+    et = np.empty(nT.value, dtype=np.int32)
+    _check(lib().fim_vtk_read(path.encode(), C.byref(nV), C.byref(nT), _ptr(xyz, C.c_double),
+                              _ptr(tets, C.c_int64), _ptr(et, C.c_int32)))
+    return xyz, tets, et
+
+
+def vtk_write(path, xyz, tets, etags=None, phi=None, states=None):
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+    tets = np.ascontiguousarray(tets, dtype=np.int64)
+    et = None if etags is None else np.ascontiguousarray(etags, dtype=np.int32)
+    ph = None if phi is None else np.ascontiguousarray(phi, dtype=np.float64)
+    sd = None if states is None else np.ascontiguousarray(states, dtype=np.float64)
+    _check(lib().fim_vtk_write(path.encode(), xyz.shape[0], tets.shape[0], _ptr(xyz, C.c_double),
+                               _ptr(tets, C.c_int64), _ptr(et, C.c_int32), _ptr(ph, C.c_double),
+                               _ptr(sd, C.c_double)))
+
+
+def read_tags(path):
+    n = C.c_int64(0)
+    _check(lib().fim_read_tags(path.encode(), C.byref(n), None))
+    tags = np.empty(n.value, dtype=np.int32)
+    _check(lib().fim_read_tags(path.encode(), C.byref(n), _ptr(tags, C.c_int32)))
+    return tags
+
+
+def load_plan(cfg_path, plan_path):
+    info = FimPlanInfo()
+    cfg = cfg_path.encode() if cfg_path else None
+    _check(lib().fim_load_plan(cfg, plan_path.encode(), C.byref(info), None))
+    stim = np.empty(info.n_stim_vertices, dtype=np.int64)
+    _check(lib().fim_load_plan(cfg, plan_path.encode(), C.byref(info), _ptr(stim, C.c_int64)))
+    return dict(dt=info.dt, n_steps=info.n_steps, n_events=info.n_events, stim=stim,
+                cv=tuple(info.cv) if info.has_cv else None, tstart=info.tstart)

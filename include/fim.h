@@ -1,0 +1,151 @@
+/*
+ * fim.h -- C ABI of the GB300 Fast Iterative Method eikonal solver.
+ *
+ * Drop-in for the solve of the reference's tw::CudaSolverFIM
+ * (src/eikonal/cuda_fim.h:1443-1577 of tomstrident/cufim-nvlink): the
+ * constructor's staging (src/eikonal/cuda_fim.cu:1218-1501) maps to
+ * fim_set_mesh / fim_set_conduction / fim_set_stimuli, CudaSolverFIM::solve
+ * (src/eikonal/cuda_fim.cu:2386-2503) maps to fim_solve + fim_get_times.
+ *
+ * Conventions
+ *  - Plain C types only; every function returns a fim_status (0 = FIM_OK).
+ *    Nothing here exits the process or throws; the message of the last error
+ *    of a solver is fim_last_error(solver) (fim_last_error(NULL) for errors
+ *    before a solver exists).
+ *  - Vertex and tet ids are int64_t as in the reference (idx_t, types.h:45).
+ *  - Times, lengths and speeds are in any consistent unit system (the
+ *    reference's files use um, um/us and us).
+ *  - A solver object is used from one host thread at a time.
+ *  - Solve semantics are those of the reference's CudaSolverFIM::solve with
+ *    every tet in one submesh: windows of length dt, n_steps of them,
+ *    narrow/next/frozen/tail states, the front-width rule and the APD reset
+ *    (src/eikonal/cuda_fim.cu:1790-1845, 1992-2334).  With dt <= 0 (or
+ *    infinite) and n_steps = 1 the solve runs to convergence in one window.
+ *    Arithmetic is FP64 with the reference's float-typed triangle
+ *    intermediates and no fused multiply-adds, so results are bit-identical
+ *    to the reference's source semantics.
+ */
+#ifndef FIM_GB300_H_
+#define FIM_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  FIM_OK = 0,
+  FIM_ERR_INVALID_ARGUMENT = 1, /* bad pointer, size, index or option       */
+  FIM_ERR_CUDA = 2,             /* a CUDA runtime call failed               */
+  FIM_ERR_NOT_READY = 3,        /* mesh / conduction / stimuli missing      */
+  FIM_ERR_TIMEOUT = 4,          /* a bounded in-kernel wait expired         */
+  FIM_ERR_MAX_ITERATIONS = 5,   /* iteration cap reached before convergence */
+  FIM_ERR_IO = 6,               /* file could not be read / written         */
+  FIM_ERR_OUT_OF_MEMORY = 7,
+  FIM_ERR_NO_DEVICE = 8
+} fim_status;
+
+/* Reference node states (types.h:85). */
+enum { FIM_FAR = 0, FIM_NEIG = 1, FIM_NARROW = 2, FIM_NEXT = 3, FIM_FROZEN = 4, FIM_TAIL = 5 };
+
+typedef struct fim_solver fim_solver;
+
+typedef struct {
+  int device;            /* CUDA device ordinal                                     */
+  double dt;             /* window length; <= 0 or inf: one window without end      */
+  int n_steps;           /* number of windows (>= 1)                                */
+  double front_width;    /* < 0: reference rule 1.01 * longest edge / 0.6           */
+  double apd;            /* frozen->tail after apd, tail->far after apd/0.91;
+                            < 0: disabled (reference: 3e5 us, cuda_fim.cu:1815)     */
+  int64_t max_iterations;/* cap on FIM iterations per window; 0: 1e7                */
+  double timeout_s;      /* limit of every in-kernel wait; <= 0: 10 s               */
+  int verbose;
+} fim_opts;
+
+/* Defaults: device 0, one endless window, reference front width, APD off. */
+void fim_default_opts(fim_opts *opts);
+
+/* Creates a solver on opts->device (NULL opts = defaults). */
+int fim_create(const fim_opts *opts, fim_solver **out);
+int fim_destroy(fim_solver *s);
+const char *fim_last_error(const fim_solver *s);
+
+/* Mesh: xyz[3*n_vertices] (x,y,z per vertex), tets[4*n_tets] (any vertex
+ * order), atags[n_tets] submesh tags or NULL.  The tags fix the reference's
+ * vertex order inside every tet (extract_submeshes2, types.cpp:306-570);
+ * NULL is one submesh.  Replaces the ctor's extract_submeshes2 and staging
+ * (cuda_fim.cu:1218-1411). */
+int fim_set_mesh(fim_solver *s, int64_t n_vertices, const double *xyz, int64_t n_tets,
+                 const int64_t *tets, const int32_t *atags);
+
+/* Conduction per tet (host pointers): unit fibre fib[3*n_tets], speed along
+ * the fibre cf[n_tets] and across it ct[n_tets].  The FP64 per-tet metric
+ * M = cf^-2 f f^T + ct^-2 (I - f f^T) and its six squared edge norms are
+ * computed on the GPU (compute_velocity_tensor_f3 + compute_geo,
+ * types.h:173-188, types.cpp:227-257; the reference hard-codes fibre (1,0,0)
+ * and 0.6 there, vtk.cpp:99-101, types.cpp:231). */
+int fim_set_conduction(fim_solver *s, const double *fib, const double *cf, const double *ct);
+/* Same, with device pointers (already resident in HBM on the solver's device). */
+int fim_set_conduction_device(fim_solver *s, const double *d_fib, const double *d_cf,
+                              const double *d_ct);
+
+/* Stimuli: n vertices with their start times (the reference seeds every
+ * stimulus at time 0, update_events_gpu, cuda_fim.cu:632-683). */
+int fim_set_stimuli(fim_solver *s, int64_t n, const int64_t *vertices, const double *t0);
+
+/* Runs the solve on `stream` (a cudaStream_t, NULL = the solver's own
+ * stream) and waits for it. */
+int fim_solve(fim_solver *s, void *stream);
+
+/* Results of the last solve: phi[n_vertices] (FP64; the reference's INF,
+ * DBL_MAX, for unreached vertices) and state[n_vertices] (or NULL). */
+int fim_get_times(fim_solver *s, double *phi, int32_t *state);
+/* Same into device memory (phi on the solver's device). */
+int fim_get_times_device(fim_solver *s, double *d_phi);
+
+typedef struct {
+  int64_t iterations;      /* FIM iterations (all windows)                  */
+  int64_t vertex_updates;  /* vertex solves (narrow + re-solved neighbours) */
+  int64_t corner_evals;    /* (vertex, tet) local solves evaluated          */
+  double solve_ms;         /* device time of the last fim_solve             */
+  double metric_ms;        /* device time of the last metric precompute     */
+  int64_t n_corners;       /* (vertex, tet) pairs of the mesh               */
+  int grid_blocks;         /* persistent grid size of the FIM kernel        */
+  int block_threads;
+} fim_stats;
+int fim_get_stats(const fim_solver *s, fim_stats *out);
+
+/* Reference-compatible files.  fim_vtk_* read/write the legacy ASCII VTK
+ * that the reference reads and writes (load_vtk / save_vtk,
+ * src/io/vtk.cpp:11-211); fim_read_tags reads a partition file
+ * (read_vector_txt, src/io/io_base.h:81-86).  Sizes-first protocol: call
+ * with NULL arrays to get the sizes, then with arrays of those sizes. */
+int fim_vtk_read(const char *path, int64_t *n_vertices, int64_t *n_tets, double *xyz,
+                 int64_t *tets, int32_t *etags);
+int fim_vtk_write(const char *path, int64_t n_vertices, int64_t n_tets, const double *xyz,
+                  const int64_t *tets, const int32_t *etags, const double *phi,
+                  const double *states);
+int fim_read_tags(const char *path, int64_t *n, int32_t *tags);
+
+/* Plan + config (load_options / load_plan, src/io/io_json.cpp:228-317):
+ * dt and n_steps (the plan's deltatime*1000 and timesteps override the cfg),
+ * stimulus vertices of the active events (sizes-first), the first region's
+ * CVref speeds (vf, vs, vn) and the first event's start time. */
+typedef struct {
+  double dt;
+  int64_t n_steps;
+  int64_t n_events;
+  int64_t n_stim_vertices;
+  double cv[3];
+  double tstart;
+  int has_cv;
+} fim_plan_info;
+int fim_load_plan(const char *cfg_path, const char *plan_path, fim_plan_info *info,
+                  int64_t *stim_vertices);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FIM_GB300_H_ */

@@ -1,0 +1,64 @@
+"""Build recipe for the oracle (test infrastructure only).
+
+* ``oracle/_build/libfim_oracle.so`` -- the C restatement in fim_oracle.c.
+* ``oracle/_ref/libfimref.so`` -- the reference's own host-compilable code
+  (local solver, preprocessing, VTK/JSON I/O) compiled from the reference
+  sources where they lie, plus ref_shim.cpp.  Built only when the reference
+  tree is present (it is not shipped with this repository).
+
+Usage: ``python oracle/build.py [--ref-root DIR]``.
+"""
+import argparse
+import os
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+DEFAULT_REF = "/root/reference"
+CUDA_INC = "/usr/local/cuda/include"
+
+
+def build_oracle(verbose=False):
+    out_dir = os.path.join(HERE, "_build")
+    os.makedirs(out_dir, exist_ok=True)
+    out = os.path.join(out_dir, "libfim_oracle.so")
+    src = os.path.join(HERE, "fim_oracle.c")
+    if os.path.exists(out) and os.path.getmtime(out) > os.path.getmtime(src):
+        return out
+    cmd = ["gcc", "-O2", "-std=c11", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared",
+           src, "-o", out, "-lm"]
+    if verbose:
+        print(" ".join(cmd))
+    subprocess.check_call(cmd)
+    return out
+
+
+def build_ref(ref_root=DEFAULT_REF, verbose=False):
+    """Compile the reference's host code into oracle/_ref/libfimref.so."""
+    if not os.path.isdir(os.path.join(ref_root, "src", "eikonal")):
+        return None
+    out_dir = os.path.join(HERE, "_ref")
+    os.makedirs(out_dir, exist_ok=True)
+    out = os.path.join(out_dir, "libfimref.so")
+    shim = os.path.join(HERE, "ref_shim.cpp")
+    srcs = [os.path.join(ref_root, "src", p) for p in (
+        "core/types.cpp", "core/logging.cpp", "core/excepts.cpp", "core/sorts.cpp",
+        "io/vtk.cpp", "io/io_json.cpp", "io/io_base.cpp")]
+    newest = max(os.path.getmtime(p) for p in srcs + [shim])
+    if os.path.exists(out) and os.path.getmtime(out) > newest:
+        return out
+    cmd = ["g++", "-std=c++17", "-O1", "-w", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared",
+           "-I" + ref_root, "-I" + os.path.join(ref_root, "src"), "-I" + CUDA_INC,
+           shim] + srcs + ["-o", out]
+    if verbose:
+        print(" ".join(cmd))
+    subprocess.check_call(cmd)
+    return out
+
+
+if __name__ == "__main__":
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref-root", default=DEFAULT_REF)
+    a = ap.parse_args()
+    print(build_oracle(verbose=True))
+    print(build_ref(a.ref_root, verbose=True))
