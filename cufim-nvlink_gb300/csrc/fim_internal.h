@@ -77,6 +77,7 @@ struct FimParams {
   double apd;           // < 0 disables the frozen->tail->far reset
   int64_t max_iter;     // per window
   uint64_t timeout_ns;  // per wait
+  int32_t withhold_block;  // test hook: block k-1 skips its first barrier arrival (0 = off)
 };
 
 // Records the message returned by fim_last_error(NULL) on this thread.

@@ -309,6 +309,9 @@ __global__ void __launch_bounds__(256) fim_solve_kernel(FimDev d, FimParams p)
   for (int64_t v = gtid; v < d.nV; v += nthreads) {
     d.phi[v] = FIM_INF; d.phi2[v] = FIM_INF; d.st[v] = ST_FAR; d.tst[v] = ST_FAR; d.flag[v] = 0;
   }
+  // failure-detection test hook: this block never arrives at the barrier (a
+  // flag that nothing sets), so the others' bounded waits must expire
+  if (p.withhold_block > 0 && (int64_t)blockIdx.x == (int64_t)p.withhold_block - 1) return;
   if (!grid_sync(ctl, nblocks, p.timeout_ns, ++where)) return;
   for (int64_t i = gtid; i < d.nseed; i += nthreads) {
     const int32_t v = d.seed_v[i];

@@ -551,6 +551,8 @@ extern "C" int fim_solve(fim_solver *s, void *stream)
   p.apd = s->opts.apd;
   p.max_iter = s->opts.max_iterations > 0 ? s->opts.max_iterations : 10000000;
   p.timeout_ns = (uint64_t)(s->opts.timeout_s * 1e9);
+  p.withhold_block = (s->opts.test_withhold_block > 0 && s->opts.test_withhold_block <= s->grid)
+                         ? s->opts.test_withhold_block : 0;
   CUDA_TRY(s, cudaMemsetAsync(s->ctl.p, 0, sizeof(FimCtl), st));
   CUDA_TRY(s, cudaEventRecord(s->ev0, st));
   CUDA_TRY(s, launch_solve(d, p, s->grid, s->block, st));

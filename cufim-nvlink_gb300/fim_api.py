@@ -30,7 +30,7 @@ EXPORTS = ["fim_default_opts", "fim_create", "fim_destroy", "fim_last_error", "f
 class FimOpts(C.Structure):
     _fields_ = [("device", C.c_int), ("dt", C.c_double), ("n_steps", C.c_int), ("front_width", C.c_double),
                 ("apd", C.c_double), ("max_iterations", C.c_int64), ("timeout_s", C.c_double),
-                ("verbose", C.c_int)]
+                ("verbose", C.c_int), ("test_withhold_block", C.c_int)]
 
 
 class FimStats(C.Structure):

@@ -62,6 +62,10 @@ typedef struct {
   int64_t max_iterations;/* cap on FIM iterations per window; 0: 1e7                */
   double timeout_s;      /* limit of every in-kernel wait; <= 0: 10 s               */
   int verbose;
+  int test_withhold_block; /* failure-detection test hook: k > 0 makes block k-1
+                              skip its first grid-barrier arrival, so the other
+                              blocks' bounded waits expire and fim_solve returns
+                              FIM_ERR_TIMEOUT; 0 = off                             */
 } fim_opts;
 
 /* Defaults: device 0, one endless window, reference front width, APD off. */
