@@ -1,0 +1,340 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 FIM eikonal solver on the anisotropic-slab workload.
+
+One step = one full solve of the slab: the FP64 per-tet metric precompute
+from the (HBM-resident) conduction field plus the persistent FIM kernel,
+i.e. everything between "conduction + stimuli given" and "activation times
+available".  Prints one JSON line (rank 0).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl mine|reference]
+
+* value      -- whole-job solves/s with inputs resident in HBM (CUDA events
+                on the solver's stream, max over ranks);
+* e2e        -- solves/s through the C ABI with pinned host buffers: H2D of
+                the conduction field + stimuli, solve, D2H of the times;
+* roofline   -- the FIM kernel's algorithmic bytes (vertex updates x
+                (40 T/V + 9) B) per launch / launch time vs measured HBM peak;
+* cpu_baseline -- the oracle (C restatement of the reference algorithm,
+                OpenMP over all host cores) on one full solve of the same slab;
+* parity     -- the last GPU result vs that FP64 oracle result.
+--gpus N > 1 runs N independent replicas (the path does not shard).
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "cufim-nvlink_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+SLAB_CELLS = (266, 93, 40)
+METRIC = "slab solves/s (1.03M-vertex anisotropic FIM, bit-exact vs FP64 oracle)"
+UNIT = "solves/s"
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["mine", "reference"], default="mine")
+    ap.add_argument("--cells", type=str, default=None, help="override slab cells, e.g. 66,23,10")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=None)
+    return ap.parse_args()
+
+
+def workload(args):
+    import fim_mesh
+    cells = tuple(int(x) for x in args.cells.split(",")) if args.cells else SLAB_CELLS
+    case = fim_mesh.slab_case(cells=cells)
+    nV, nT = case["xyz"].shape[0], case["tets"].shape[0]
+    cfg = {
+        "workload": (f"anisotropic slab 20x7x3 mm, {cells[0]}x{cells[1]}x{cells[2]} Kuhn cells "
+                     f"({nV} vertices, {nT} tets), +-0.2h jitter, fibres -60..+60 deg over z, cf 0.6 / "
+                     "ct 0.24 mm/ms, 2 mm scar x0.1, 5 surface stimuli t0~U[0,10] ms; one submesh, "
+                     "one endless window"),
+        "vertices": nV, "tets": nT, "seed": 2,
+        "l2": "inputs larger than L2 (corner records 96 B x 4T)",
+        "parallelism": "replicas",
+    }
+    return case, cfg
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        import torch
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend=backend)
+        pg = dist
+    return world, rank, local, pg
+
+
+def max_over_ranks(pg, value, device=None):
+    if pg is None:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", "--query-gpu=" + self.QUERY, "--format=csv,noheader,nounits",
+                                          "-lms", "100"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+            t0 = time.time()
+            while time.time() - t0 < 3.0 and os.path.getsize(self.path) == 0:
+                time.sleep(0.05)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                if int(f[0]) != self.index:
+                    continue
+                rows.append(f)
+            except ValueError:
+                continue
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ---------------------------------------------------------------------------
+# CPU oracle (checker + CPU baseline): the C restatement of the reference's
+# algorithm, OpenMP over every host core
+def oracle_solve(case, threads=0):
+    from oracle import build as obuild
+    obuild.build_oracle()
+    from oracle import oracle as O
+    nV = case["xyz"].shape[0]
+    t0 = time.perf_counter()
+    slots, _, _, _ = O.reference_slots(nV, case["tets"], None)
+    t1 = time.perf_counter()
+    geo = O.metric_geo(slots, case["xyz"], case["fib"], case["cf"], case["ct"])
+    phi, st, it, upd = O.solve_pure(nV, slots, geo, case["seed_v"], case["seed_t"], threads=threads)
+    t2 = time.perf_counter()
+    return phi, st, {"solve_s": t2 - t1, "prep_s": t1 - t0, "iterations": it, "vertex_updates": upd}
+
+
+def parity_report(phi, phi_o):
+    finite = phi_o < 1e300
+    tmax = float(phi_o[finite].max()) if finite.any() else 1.0
+    d = np.abs(np.where(finite, phi, 0.0) - np.where(finite, phi_o, 0.0))
+    same_inf = bool(np.array_equal(phi >= 1e300, ~finite))
+    return {"max_abs_err": float(d.max()), "max_rel_err": float(d.max() / tmax),
+            "rms_rel_err": float(np.sqrt(np.mean(d ** 2)) / tmax),
+            "n_bit_mismatch": int(np.count_nonzero(phi != phi_o)), "unreached_match": same_inf,
+            "tolerance": "max |dt| <= 1e-4 max(t); achieved bit-exact"}
+
+
+def run_mine(args):
+    import torch
+    import fim_api
+    world, rank, local, pg = dist_setup(args)
+    dev = torch.device(f"cuda:{local}")
+    torch.cuda.set_device(dev)
+    case, cfg = workload(args)
+    nV, nT = case["xyz"].shape[0], case["tets"].shape[0]
+    peaks = {}
+    pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(pk):
+        peaks = json.load(open(pk))
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+
+    s = fim_api.Solver(device=local)
+    s.set_mesh(case["xyz"], case["tets"])
+    stream = torch.cuda.Stream(dev)
+    s.set_stream(stream.cuda_stream)
+    fib = torch.tensor(case["fib"], dtype=torch.float64, device=dev).contiguous()
+    cf = torch.tensor(case["cf"], dtype=torch.float64, device=dev)
+    ct = torch.tensor(case["ct"], dtype=torch.float64, device=dev)
+    s.set_stimuli(case["seed_v"], case["seed_t"])
+    torch.cuda.synchronize()
+
+    solve_ms, metric_ms = [], []
+
+    def step(record):
+        s.set_conduction_device(fib.data_ptr(), cf.data_ptr(), ct.data_ptr())
+        s.solve()
+        if record:
+            st = s.stats()
+            solve_ms.append(st["solve_ms"])
+            metric_ms.append(st["metric_ms"])
+
+    for _ in range(max(args.warmup, 0)):
+        step(False)
+    clocks = ClockSampler(index=local)
+    clocks.start()
+    barrier(pg)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        step(True)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    barrier(pg)
+    clk = clocks.stop()
+    dev_ms = ev0.elapsed_time(ev1)
+    max_ms = max_over_ranks(pg, dev_ms, dev if pg is not None and torch.cuda.is_available() else None)
+    stats = s.stats()
+    phi_dev = s.times(with_state=False)
+
+    # end to end through the C ABI from pinned host buffers
+    e2e_steps = args.e2e_steps or max(3, min(args.steps, 10))
+    h_fib = torch.from_numpy(case["fib"]).pin_memory().numpy()
+    h_cf = torch.from_numpy(case["cf"]).pin_memory().numpy()
+    h_ct = torch.from_numpy(case["ct"]).pin_memory().numpy()
+    h_sv = torch.from_numpy(case["seed_v"].astype(np.int64)).pin_memory().numpy()
+    h_st = torch.from_numpy(case["seed_t"]).pin_memory().numpy()
+    h_phi = torch.empty(nV, dtype=torch.float64).pin_memory().numpy()
+    import ctypes as C
+    L = fim_api.lib()
+    P = fim_api._ptr
+
+    def e2e_step():
+        fim_api._check(L.fim_set_conduction(s.h, P(h_fib, C.c_double), P(h_cf, C.c_double), P(h_ct, C.c_double)), s.h)
+        fim_api._check(L.fim_set_stimuli(s.h, h_sv.shape[0], P(h_sv, C.c_int64), P(h_st, C.c_double)), s.h)
+        fim_api._check(L.fim_solve(s.h, None), s.h)
+        fim_api._check(L.fim_get_times(s.h, P(h_phi, C.c_double), None), s.h)
+
+    e2e_step()
+    barrier(pg)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_step()
+    e2e_s = max_over_ranks(pg, time.perf_counter() - t0, dev if pg is not None and torch.cuda.is_available() else None)
+    barrier(pg)
+    h2d = h_fib.nbytes + h_cf.nbytes + h_ct.nbytes + h_sv.nbytes + h_st.nbytes
+    d2h = h_phi.nbytes
+    assert np.array_equal(h_phi, phi_dev)
+
+    if rank != 0:
+        s.close()
+        return
+    b_vu = 40.0 * nT / nV + 9.0
+    upd = stats["vertex_updates"]
+    mean_solve_ms = float(np.mean(solve_ms))
+    achieved = upd * b_vu / (mean_solve_ms * 1e-3) / 1e9
+    out = {
+        "metric": METRIC, "value": world * args.steps / (max_ms * 1e-3), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": max_ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded slab mesh, conduction field and stimuli)", "config": cfg,
+        "solve_ms": mean_solve_ms, "metric_ms": float(np.mean(metric_ms)),
+        "iterations": stats["iterations"], "vertex_updates": upd,
+        "vertex_updates_per_s": upd / (mean_solve_ms * 1e-3), "corners_screened": stats["corner_evals"],
+        "fp64_local_solves": stats["exact_evals"],
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": achieved / hbm_peak, "traffic": None,
+                     "kernel": "fim_solve_kernel", "bytes_per_vertex_update": b_vu,
+                     "peak_source": peak_src,
+                     "note": "FP64-pipe bound on GB300; algorithmic bytes per SURVEY model"},
+        "e2e": {"value": world * e2e_steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": 2 * args.steps,
+        "clocks": clk,
+    }
+    if world == 1 and not args.no_cpu_baseline:
+        phi_o, _, ost = oracle_solve(case)
+        cores = os.cpu_count()
+        out["cpu_baseline"] = {"value": 1.0 / ost["solve_s"], "unit": UNIT, "cores": cores, "kind": "port",
+                               "sample": "one full solve of the same slab (metric + FIM) by the FP64 C oracle"}
+        out["parity"] = parity_report(phi_dev, phi_o)
+    s.close()
+    print(json.dumps(out), flush=True)
+
+
+def run_reference(args):
+    """The reference's algorithm on the host cores: the oracle port (the
+    reference's own solver is CUDA-only; its CPU twins are commented out and
+    its sources are not present on the GPU machine)."""
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    case, cfg = workload(args)
+    for _ in range(max(args.warmup, 0)):
+        oracle_solve(case)
+    t = 0.0
+    for _ in range(args.steps):
+        _, _, ost = oracle_solve(case)
+        t += ost["solve_s"]
+    value = args.steps / t
+    cores = os.cpu_count()
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded slab mesh, conduction field and stimuli)", "config": cfg,
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": "one full solve of the slab per step (metric + FIM), FP64 C oracle, OpenMP"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_mine(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -29,6 +29,7 @@ struct FimCtl {
   int64_t iterations;
   int64_t vertex_updates;
   int64_t corner_evals;
+  int64_t exact_evals;
 };
 
 // Everything the persistent kernel touches, as device pointers.
@@ -51,6 +52,8 @@ struct FimDev {
   const int64_t *cptr;        // [nV+1] corner range per vertex
   const int4 *cids;           // [nC] other three vertices of the corner ("1","2","3"), w unused
   const double *cgeo;         // [nC*10] e13,e23,e34,e12,e14,e24, sqrt(e14), sqrt(e24), sqrt(e34), pad
+  const float *cgf;           // [nC*12] float screen record: e13..e24 * 2^-k, sqrt(e14,e24,e34), k, bad, pad
+  float *phi_f;               // float copy (round to nearest) of phi, kept in step with it
   const int64_t *nptr;        // [nV+1] vertex neighbourhood (self included)
   const int32_t *nbr;
   // state
@@ -78,6 +81,7 @@ struct FimParams {
   int64_t max_iter;     // per window
   uint64_t timeout_ns;  // per wait
   int32_t withhold_block;  // test hook: block k-1 skips its first barrier arrival (0 = off)
+  int32_t exact_all;       // 1: every local solve in FP64, no interval filter
 };
 
 // Records the message returned by fim_last_error(NULL) on this thread.
@@ -87,7 +91,7 @@ void set_last_error(const char *msg);
 // FP64 metric + edge norms per tet scattered into the corner records.
 cudaError_t launch_metric(const int32_t *tslots, const int64_t *cidx, const double *xyz,
                           const double *fib, const double *cf, const double *ct, int64_t nT,
-                          double *cgeo, cudaStream_t stream);
+                          double *cgeo, float *cgf, cudaStream_t stream);
 // Persistent cooperative solve.
 cudaError_t launch_solve(const FimDev &d, const FimParams &p, int grid, int block, cudaStream_t stream);
 // Occupancy-derived grid size for the cooperative launch.

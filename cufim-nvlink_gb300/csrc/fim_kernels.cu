@@ -22,6 +22,7 @@
 //    compacted lists (narrow list, vertices frozen this iteration,
 //    neighbours to re-solve), separated by a bounded grid barrier.
 #include "fim_internal.h"
+#include "fim_filter.cuh"
 
 #include <cfloat>
 #include <cstdint>
@@ -98,25 +99,6 @@ __device__ __forceinline__ double tet_ref(double e13, double e23, double e34, do
   return fmin(ra, rb);
 }
 
-// update_per_element (cuda_fim.h:1362-1411) for one corner.  A branch whose
-// neighbours are not all valid is skipped: with the reference's INF
-// (DBL_MAX) operands such a branch never produces a value below the others
-// (checked against the reference's own code on 3e5 random corners), so the
-// result is identical.  g: e13,e23,e34,e12,e14,e24,sqrt(e14),sqrt(e24),sqrt(e34).
-__device__ __forceinline__ double corner_candidate(const double *g, double p1, double p2, double p3,
-                                                   bool v1, bool v2, bool v3)
-{
-  double r = FIM_INF;
-  if (v1 && v2 && v3) r = tet_ref(g[0], g[1], g[2], g[3], g[4], g[5], p1, p2, p3);
-  if (v1 && v2) r = fmin(r, tri_ref(g[3], g[4], g[5], p1, p2));
-  if (v2 && v3) r = fmin(r, tri_ref(g[1], g[5], g[2], p2, p3));
-  if (v1 && v3) r = fmin(r, tri_ref(g[0], g[4], g[2], p1, p3));
-  if (v1) r = fmin(r, p1 + g[6]);
-  if (v2) r = fmin(r, p2 + g[7]);
-  if (v3) r = fmin(r, p3 + g[8]);
-  return r;
-}
-
 // ---------------------------------------------------------------------------
 // metric kernel
 
@@ -143,7 +125,7 @@ __host__ __device__ constexpr int sel_of(int t, int k)
 __global__ void fim_metric_kernel(const int32_t *__restrict__ tslots, const int64_t *__restrict__ cidx,
                                   const double *__restrict__ xyz, const double *__restrict__ fib,
                                   const double *__restrict__ cf, const double *__restrict__ ct,
-                                  int64_t nT, double *__restrict__ cgeo)
+                                  int64_t nT, double *__restrict__ cgeo, float *__restrict__ cgf)
 {
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nT;
        e += (int64_t)gridDim.x * blockDim.x) {
@@ -170,13 +152,28 @@ __global__ void fim_metric_kernel(const int32_t *__restrict__ tslots, const int6
       g[k] = (M0*ex + M1*ey + M2*ez)*ex + (M1*ex + M3*ey + M4*ez)*ey + (M2*ex + M4*ey + M5*ez)*ez;
       s[k] = sqrt(g[k]);
     }
+    // scale 2^-k (k even) of the float screen record: edge norms O(1)
+    double gmax = g[0];
+#pragma unroll
+    for (int kk = 1; kk < 6; ++kk) gmax = fmax(gmax, g[kk]);
+    int ex = 0;
+    frexp(gmax, &ex);
+    int ks = ex & ~1;
+    const bool ok = isfinite(gmax) && gmax > 0.0 && ks <= 50 && ks >= -50;
+    if (!ok) ks = 0;
+    const double sg = ldexp(1.0, -ks);
 #pragma unroll
     for (int t = 0; t < 4; ++t) {
-      double *o = cgeo + 10 * cidx[4 * e + t];
+      const int64_t c = cidx[4 * e + t];
+      double *o = cgeo + 10 * c;
       o[0] = g[sel_of(t, 0)]; o[1] = g[sel_of(t, 1)]; o[2] = g[sel_of(t, 2)];
       o[3] = g[sel_of(t, 3)]; o[4] = g[sel_of(t, 4)]; o[5] = g[sel_of(t, 5)];
       o[6] = s[sel_of(t, 4)]; o[7] = s[sel_of(t, 5)]; o[8] = s[sel_of(t, 2)];
       o[9] = 0.0;
+      float4 *of = reinterpret_cast<float4 *>(cgf + 12 * c);
+      of[0] = make_float4((float)(o[0] * sg), (float)(o[1] * sg), (float)(o[2] * sg), (float)(o[3] * sg));
+      of[1] = make_float4((float)(o[4] * sg), (float)(o[5] * sg), (float)o[6], (float)o[7]);
+      of[2] = make_float4((float)o[8], (float)ks, ok ? 0.f : 1.f, 0.f);
     }
   }
 }
@@ -257,39 +254,260 @@ struct WarpCtx {
   int64_t nwarps;
 };
 
-// New time of vertex v from all its corners (one warp, lanes over corners):
-// min over the candidates of update_per_element with the reference's
-// validity rule (state >= narrow and phi > phi_start - front_width,
-// cuda_fim.h:1375-1383).  Returns the warp-wide minimum on every lane.
-__device__ __forceinline__ double warp_vertex_update(const FimDev &d, int32_t v, double lower,
-                                                     int lane, int64_t &evals)
+// One FP64 local solve of the reference for corner c: kind 0..2 are the
+// triangle solves (1,2), (2,3), (1,3) and kind 3 the tet solve.  The caller
+// guarantees the neighbours the solve uses are valid.
+__device__ double exact_candidate(const FimDev &d, int64_t c, int kind)
 {
+  const int4 id = __ldg(d.cids + c);
+  const double p1 = __ldcg(d.phi + id.x), p2 = __ldcg(d.phi + id.y), p3 = __ldcg(d.phi + id.z);
+  const double2 *gp = reinterpret_cast<const double2 *>(d.cgeo + 10 * c);
+  double g[6];
+  {
+    const double2 t0 = __ldg(gp), t1 = __ldg(gp + 1), t2 = __ldg(gp + 2);
+    g[0] = t0.x; g[1] = t0.y; g[2] = t1.x; g[3] = t1.y; g[4] = t2.x; g[5] = t2.y;
+  }
+  if (kind == 3) return tet_ref(g[0], g[1], g[2], g[3], g[4], g[5], p1, p2, p3);
+  if (kind == 0) return tri_ref(g[3], g[4], g[5], p1, p2);
+  if (kind == 1) return tri_ref(g[1], g[5], g[2], p2, p3);
+  return tri_ref(g[0], g[4], g[2], p1, p3);
+}
+
+// Order-preserving map of doubles to unsigned integers, so that the minimum
+// of a vertex's candidates can be formed with integer atomicMin.
+__device__ __forceinline__ unsigned long long dkey(double x)
+{
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double dunkey(unsigned long long k)
+{
+  const unsigned long long b = (k >> 63) ? (k & 0x7fffffffffffffffull) : ~k;
+  return __longlong_as_double((long long)b);
+}
+
+constexpr int kWarps = 8;            // warps per block (256 threads)
+constexpr int kMaxVpw = 8;           // vertices per warp per batch
+constexpr int kSlots = kWarps * kMaxVpw;
+constexpr int kQcap = 1024;          // exact solves queued per kind and batch
+
+// Shared memory of one batch of vertex updates.
+struct BatchSh {
+  int32_t vtx[kSlots];
+  int64_t c0[kSlots];
+  double old[kSlots];
+  unsigned long long res[kSlots];  // dkey of the running minimum
+  uint32_t q[2][kQcap];            // queued exact solves: [0] tets, [1] triangles
+  int nq[2];
+};
+
+// Queue item: slot (6 bits) | kind (2 bits) | corner offset in the vertex (24 bits).
+__device__ __forceinline__ uint32_t make_item(int slot, int kind, int64_t off)
+{
+  return (uint32_t)slot | ((uint32_t)kind << 6) | ((uint32_t)off << 8);
+}
+
+// Screens all corners of vertex v (one warp, lanes over corners).  First
+// pass: float bounds of the edge candidates give an upper bound bhi of the
+// vertex's new time; the edge candidates that can still be the minimum are
+// added exactly (one FP64 add each).  Second pass: triangle and tet solves
+// whose trivial bound min(neighbour times) is below bhi are screened
+// (fim_filter.cuh); those that can still be the minimum are queued for the
+// exact FP64 solve.  The minimum of everything equals the reference's
+// update_per_element minimum over all corners (cuda_fim.h:1362-1411), with
+// the validity rule state >= narrow and phi > phi_start - front_width; the
+// rule is decided on the float copies when they are conclusive and on the
+// FP64 times otherwise.
+__device__ void warp_filter_vertex(const FimDev &d, BatchSh &sh, int slot, int32_t v, double lower,
+                                   float lower_lo, float lower_hi, bool exact_all, int lane, int64_t &n_filtered)
+{
+  const double old = __ldcg(d.phi + v);
   const int64_t c0 = d.cptr[v], c1 = d.cptr[v + 1];
-  double best = FIM_INF;
-  for (int64_t c = c0 + lane; c < c1; c += 32) {
-    const int4 id = __ldg(d.cids + c);
-    const double p1 = __ldcg(d.phi + id.x), p2 = __ldcg(d.phi + id.y), p3 = __ldcg(d.phi + id.z);
-    const uint8_t s1 = __ldcg(d.st + id.x), s2 = __ldcg(d.st + id.y), s3 = __ldcg(d.st + id.z);
-    const bool v1 = (s1 >= ST_NARROW) && (p1 > lower);
-    const bool v2 = (s2 >= ST_NARROW) && (p2 > lower);
-    const bool v3 = (s3 >= ST_NARROW) && (p3 > lower);
-    if (v1 || v2 || v3) {
-      const double2 *gp = reinterpret_cast<const double2 *>(d.cgeo + 10 * c);
-      double g[10];
+  if (lane == 0) { sh.vtx[slot] = v; sh.c0[slot] = c0; sh.old[slot] = old; sh.res[slot] = dkey(old); }
+  float bhi = exact_all ? INFINITY : re_hi(re_in(__ldcg(d.phi_f + v)));
+  for (int64_t cc = c0; cc < c1; cc += 32) {
+    const int64_t c = cc + lane;
+    bool vv[3] = {false, false, false};
+    Re P[3];
+    float4 r0 = make_float4(0.f, 0.f, 0.f, 0.f), r1 = r0, r2 = r0;
+    int4 id = make_int4(0, 0, 0, 0);
+    float lbE[3] = {INFINITY, INFINITY, INFINITY};
+    float ub = INFINITY;
+    if (c < c1) {
+      id = __ldg(d.cids + c);
+      const int32_t nb[3] = {id.x, id.y, id.z};
 #pragma unroll
-      for (int k = 0; k < 5; ++k) {
-        const double2 t = __ldg(gp + k);
-        g[2 * k] = t.x;
-        g[2 * k + 1] = t.y;
+      for (int i = 0; i < 3; ++i) {
+        const float pf = __ldcg(d.phi_f + nb[i]);
+        P[i] = re_in(pf);
+        bool ok = __ldcg(d.st + nb[i]) >= ST_NARROW;
+        if (ok) {
+          if (re_lo(P[i]) > lower_hi) ok = true;
+          else if (re_hi(P[i]) <= lower_lo) ok = false;
+          else ok = __ldcg(d.phi + nb[i]) > lower;
+        }
+        vv[i] = ok;
       }
-      best = fmin(best, corner_candidate(g, v1 ? p1 : FIM_INF, v2 ? p2 : FIM_INF, v3 ? p3 : FIM_INF,
-                                         v1, v2, v3));
-      ++evals;
+      if (vv[0] || vv[1] || vv[2]) {
+        ++n_filtered;
+        const float4 *rp = reinterpret_cast<const float4 *>(d.cgf + 12 * c);
+        r0 = __ldg(rp);
+        r1 = __ldg(rp + 1);
+        r2 = __ldg(rp + 2);
+        const float sv[3] = {r1.z, r1.w, r2.x};
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+          if (vv[i]) {
+            const Re E = P[i] + re_in(sv[i]);
+            lbE[i] = re_lo(E);
+            ub = fminf(ub, re_hi(E));
+          }
+      }
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) ub = fminf(ub, __shfl_xor_sync(FULL_MASK, ub, off));
+    if (!exact_all) bhi = fminf(bhi, ub);
+    // exact edge candidates that can still be the minimum
+    if (c < c1) {
+      const int32_t nb[3] = {id.x, id.y, id.z};
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+        if (vv[i] && !(lbE[i] > bhi)) {
+          const double val = __ldcg(d.phi + nb[i]) + __ldg(d.cgeo + 10 * c + 6 + i);
+          atomicMin(&sh.res[slot], dkey(val));
+        }
+    }
+    // triangle and tet screens
+    CandBound cb[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) { cb[k].some = CAND_NONE; cb[k].lb = NAN; cb[k].ub = INFINITY; }
+    float ub2 = INFINITY;
+    if (c < c1 && (vv[0] || vv[1] || vv[2])) {
+      const bool bad = exact_all || r2.z != 0.f;
+      const int ks = (int)r2.y;
+      const float tk = re_pow2f(ks);
+      const Re gs[6] = {re_in(r0.x), re_in(r0.y), re_in(r0.z), re_in(r0.w), re_in(r1.x), re_in(r1.y)};
+      const float lo0 = re_lo(P[0]), lo1 = re_lo(P[1]), lo2 = re_lo(P[2]);
+      // pairs (1,2), (2,3), (1,3): kind 0, 1, 2
+      if (vv[0] && vv[1] && !(fminf(lo0, lo1) > bhi)) {
+        if (bad) cb[0].some = CAND_SOME;
+        else cb[0] = tri_screen(re_scale(gs[3], tk), re_scale(gs[4], tk), re_scale(gs[5], tk), P[0], P[1]);
+      }
+      if (vv[1] && vv[2] && !(fminf(lo1, lo2) > bhi)) {
+        if (bad) cb[1].some = CAND_SOME;
+        else cb[1] = tri_screen(re_scale(gs[1], tk), re_scale(gs[5], tk), re_scale(gs[2], tk), P[1], P[2]);
+      }
+      if (vv[0] && vv[2] && !(fminf(lo0, lo2) > bhi)) {
+        if (bad) cb[2].some = CAND_SOME;
+        else cb[2] = tri_screen(re_scale(gs[0], tk), re_scale(gs[4], tk), re_scale(gs[2], tk), P[0], P[2]);
+      }
+      if (vv[0] && vv[1] && vv[2] && !(fminf(lo0, fminf(lo1, lo2)) > bhi)) {
+        if (bad) cb[3].some = CAND_SOME;
+        else cb[3] = tet_screen(gs, P[0], P[1], P[2], ks);
+      }
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        if (cb[k].some) ub2 = fminf(ub2, cb[k].ub);
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) ub2 = fminf(ub2, __shfl_xor_sync(FULL_MASK, ub2, off));
+    if (!exact_all) bhi = fminf(bhi, ub2);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const bool need = cb[k].some && !(cb[k].lb > bhi);
+      const unsigned mask = __ballot_sync(FULL_MASK, need);
+      if (mask == 0) continue;
+      const int qi = (k == 3) ? 0 : 1;
+      int base = 0;
+      if (lane == 0) base = atomicAdd(&sh.nq[qi], __popc(mask));
+      base = __shfl_sync(FULL_MASK, base, 0);
+      if (need) {
+        const int pos = base + __popc(mask & ((1u << lane) - 1u));
+        if (pos < kQcap) {
+          sh.q[qi][pos] = make_item(slot, k, c - c0);
+        } else {  // queue full: solve here
+          const double val = exact_candidate(d, c, k);
+          if (val < FIM_INF) atomicMin(&sh.res[slot], dkey(val));
+        }
+      }
     }
   }
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1) best = fmin(best, __shfl_xor_sync(FULL_MASK, best, off));
-  return best;
+}
+
+// Writes a time and its float copy.
+__device__ __forceinline__ void set_phi(const FimDev &d, int64_t v, double x)
+{
+  d.phi[v] = x;
+  d.phi_f[v] = (float)x;
+}
+
+// Solves the queued exact candidates of the batch with all threads of the
+// block (tets first, then triangles, each loop uniform in its work).
+__device__ void block_drain(const FimDev &d, BatchSh &sh, int64_t &n_exact)
+{
+#pragma unroll 1
+  for (int qi = 0; qi < 2; ++qi) {
+    const int n = min(sh.nq[qi], kQcap);
+    for (int j = threadIdx.x; j < n; j += blockDim.x) {
+      const uint32_t it = sh.q[qi][j];
+      const int slot = it & 63, kind = (it >> 6) & 3;
+      const int64_t c = sh.c0[slot] + (int64_t)(it >> 8);
+      const double val = exact_candidate(d, c, kind);
+      ++n_exact;
+      if (val < FIM_INF) atomicMin(&sh.res[slot], dkey(val));
+    }
+  }
+}
+
+// One update phase over a vertex list, processed in block batches: every
+// warp filters its vertices, the block then solves the queued exact
+// candidates of the whole batch with full warps, and finally applies the
+// reference's per-vertex decision.
+//  mode 0 -- narrow vertices: reduce per vertex, window test (next), freeze
+//            test (cuda_fim.cu:2125-2163);
+//  mode 1 -- re-solved neighbours: reduce and keep the decided state
+//            (cuda_fim.cu:2255-2289).
+__device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, int32_t n, int mode, double lower,
+                             float lower_lo, float lower_hi, double phi_start, double dt, bool exact_all, int s,
+                             int64_t &n_filtered, int64_t &n_exact)
+{
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t total_warps = (int64_t)gridDim.x * kWarps;
+  int vpw = (int)((n + total_warps - 1) / total_warps);
+  vpw = max(1, min(kMaxVpw, vpw));
+  const int nb = kWarps * vpw;
+  for (int64_t base = (int64_t)blockIdx.x * nb; base < n; base += (int64_t)gridDim.x * nb) {
+    if (threadIdx.x == 0) { sh.nq[0] = 0; sh.nq[1] = 0; }
+    __syncthreads();
+    const int nslot = (int)min((int64_t)nb, (int64_t)n - base);
+    for (int j = 0; j < vpw; ++j) {
+      const int slot = warp * vpw + j;
+      if (slot < nslot)
+        warp_filter_vertex(d, sh, slot, __ldcg(list + base + slot), lower, lower_lo, lower_hi, exact_all, lane,
+                           n_filtered);
+    }
+    __syncthreads();
+    block_drain(d, sh, n_exact);
+    __syncthreads();
+    for (int slot = threadIdx.x; slot < nslot; slot += blockDim.x) {
+      const int32_t v = sh.vtx[slot];
+      const double old = sh.old[slot];
+      const double nw = dunkey(sh.res[slot]);
+      d.phi2[v] = nw;
+      if (mode == 0) {
+        d.tst[v] = ST_FAR;
+        if (nw - phi_start > dt) {
+          d.st[v] = ST_NEXT;
+        } else if (fabs(old - nw) < (1e-6 * (1 + (old + nw) * .5))) {
+          d.tst[v] = ST_FROZEN;
+          d.lfrozen[atomicAdd(&d.ctl->n_frozen[s], 1)] = v;
+        }
+      } else {
+        d.dec[base + slot] = (nw < old) ? (uint8_t)ST_NARROW : __ldcg(d.tst + v);
+      }
+    }
+    __syncthreads();
+  }
 }
 
 __global__ void __launch_bounds__(256) fim_solve_kernel(FimDev d, FimParams p)
@@ -302,12 +520,13 @@ __global__ void __launch_bounds__(256) fim_solve_kernel(FimDev d, FimParams p)
   w.lane = threadIdx.x & 31;
   w.gwarp = gtid >> 5;
   w.nwarps = nthreads >> 5;
-  int64_t my_evals = 0, my_updates = 0;
+  int64_t my_evals = 0, my_updates = 0, my_exact = 0;
   int where = 0;
+  __shared__ BatchSh sh;
 
   // reset_states_gpu + update_events_gpu: phi = INF, far; seeds narrow.
   for (int64_t v = gtid; v < d.nV; v += nthreads) {
-    d.phi[v] = FIM_INF; d.phi2[v] = FIM_INF; d.st[v] = ST_FAR; d.tst[v] = ST_FAR; d.flag[v] = 0;
+    set_phi(d, v, FIM_INF); d.phi2[v] = FIM_INF; d.st[v] = ST_FAR; d.tst[v] = ST_FAR; d.flag[v] = 0;
   }
   // failure-detection test hook: this block never arrives at the barrier (a
   // flag that nothing sets), so the others' bounded waits must expire
@@ -315,7 +534,7 @@ __global__ void __launch_bounds__(256) fim_solve_kernel(FimDev d, FimParams p)
   if (!grid_sync(ctl, nblocks, p.timeout_ns, ++where)) return;
   for (int64_t i = gtid; i < d.nseed; i += nthreads) {
     const int32_t v = d.seed_v[i];
-    d.phi[v] = d.seed_t[i]; d.phi2[v] = d.seed_t[i]; d.st[v] = ST_NARROW;
+    set_phi(d, v, d.seed_t[i]); d.phi2[v] = d.seed_t[i]; d.st[v] = ST_NARROW;
   }
   if (!grid_sync(ctl, nblocks, p.timeout_ns, ++where)) return;
 
@@ -325,6 +544,7 @@ __global__ void __launch_bounds__(256) fim_solve_kernel(FimDev d, FimParams p)
     phi_start = cur_time;
     cur_time += p.dt;
     const double lower = phi_start - p.front_width;
+    const float lower_lo = __double2float_rd(lower), lower_hi = __double2float_ru(lower);
     int s = (int)(it % 3);
     if (gtid == 0) {
       for (int k = 0; k < 3; ++k) { ctl->n_narrow[k] = 0; ctl->n_frozen[k] = 0; ctl->n_marked[k] = 0; }
@@ -344,7 +564,7 @@ __global__ void __launch_bounds__(256) fim_solve_kernel(FimDev d, FimParams p)
         }
         for (int64_t k = k0; k < k1; ++k) {
           const int32_t c = d.gcopy[k];
-          if (mn < __ldcg(d.phi + c)) { d.phi[c] = mn; d.phi2[c] = mn; d.st[c] = ST_NARROW; }
+          if (mn < __ldcg(d.phi + c)) { set_phi(d, c, mn); d.phi2[c] = mn; d.st[c] = ST_NARROW; }
         }
       }
     }
@@ -357,7 +577,7 @@ __global__ void __launch_bounds__(256) fim_solve_kernel(FimDev d, FimParams p)
         if (!(d.phi[v] + p.apd > cur_time)) d.st[v] = ST_TAIL;
       } else if (p.apd >= 0.0 && stv == ST_TAIL) {
         if (!(d.phi[v] + p.apd / 0.91 > cur_time)) {
-          d.phi[v] = FIM_INF; d.phi2[v] = FIM_INF; d.st[v] = ST_FAR;
+          set_phi(d, v, FIM_INF); d.phi2[v] = FIM_INF; d.st[v] = ST_FAR;
         }
       }
       if (stv == ST_NARROW) d.list[s][atomicAdd(&ctl->n_narrow[s], 1)] = (int32_t)v;
@@ -380,22 +600,7 @@ __global__ void __launch_bounds__(256) fim_solve_kernel(FimDev d, FimParams p)
       if (gtid == 0) { ctl->n_narrow[s2] = 0; ctl->n_frozen[s2] = 0; ctl->n_marked[s2] = 0; }
 
       // P1 -- solve on elements + reduce per vertex (cuda_fim.cu:2102-2163)
-      for (int64_t i = w.gwarp; i < nn; i += w.nwarps) {
-        const int32_t v = lst[i];
-        const double best = warp_vertex_update(d, v, lower, w.lane, my_evals);
-        if (w.lane == 0) {
-          const double old = __ldcg(d.phi + v);
-          const double nw = (best < old) ? best : old;
-          d.phi2[v] = nw;
-          d.tst[v] = ST_FAR;
-          if (nw - phi_start > p.dt) {
-            d.st[v] = ST_NEXT;
-          } else if (fabs(old - nw) < (1e-6 * (1 + (old + nw) * .5))) {
-            d.tst[v] = ST_FROZEN;
-            d.lfrozen[atomicAdd(&ctl->n_frozen[s], 1)] = v;
-          }
-        }
-      }
+      update_phase(d, sh, lst, nn, 0, lower, lower_lo, lower_hi, phi_start, p.dt, p.exact_all != 0, s, my_evals, my_exact);
       my_updates += (gtid == 0) ? nn : 0;
       if (!grid_sync(ctl, nblocks, p.timeout_ns, ++where)) return;
 
@@ -403,7 +608,7 @@ __global__ void __launch_bounds__(256) fim_solve_kernel(FimDev d, FimParams p)
       // vertices frozen now (cuda_fim.cu:2172-2205)
       for (int64_t i = gtid; i < nn; i += nthreads) {
         const int32_t v = lst[i];
-        d.phi[v] = __ldcg(d.phi2 + v);
+        set_phi(d, v, __ldcg(d.phi2 + v));
       }
       const int32_t nf = ld_volatile_i32(&ctl->n_frozen[s]);
       for (int64_t i = w.gwarp; i < nf; i += w.nwarps) {
@@ -424,23 +629,14 @@ __global__ void __launch_bounds__(256) fim_solve_kernel(FimDev d, FimParams p)
 
       // P3 -- solve elements for neighbours + reduce (cuda_fim.cu:2215-2289)
       const int32_t nm = ld_volatile_i32(&ctl->n_marked[s]);
-      for (int64_t i = w.gwarp; i < nm; i += w.nwarps) {
-        const int32_t v = d.lmarked[i];
-        const double best = warp_vertex_update(d, v, lower, w.lane, my_evals);
-        if (w.lane == 0) {
-          const double old = __ldcg(d.phi + v);
-          const double nw = (best < old) ? best : old;
-          d.phi2[v] = nw;
-          d.dec[i] = (nw < old) ? (uint8_t)ST_NARROW : __ldcg(d.tst + v);
-        }
-      }
+      update_phase(d, sh, d.lmarked, nm, 1, lower, lower_lo, lower_hi, phi_start, p.dt, p.exact_all != 0, s, my_evals, my_exact);
       my_updates += (gtid == 0) ? nm : 0;
       if (!grid_sync(ctl, nblocks, p.timeout_ns, ++where)) return;
 
       // P4 -- apply, update neighbour states, next narrow list (cuda_fim.cu:2291-2317)
       for (int64_t i = gtid; i < nm; i += nthreads) {
         const int32_t v = d.lmarked[i];
-        d.phi[v] = __ldcg(d.phi2 + v);
+        set_phi(d, v, __ldcg(d.phi2 + v));
         uint8_t sv = __ldcg(d.dec + i);
         if (sv == ST_NARROW) {
           if (__ldcg(d.tst + v) == ST_FROZEN) sv = ST_FROZEN;
@@ -480,12 +676,16 @@ __global__ void __launch_bounds__(256) fim_solve_kernel(FimDev d, FimParams p)
   }
 
   // statistics
-  __shared__ unsigned long long s_evals;
-  if (threadIdx.x == 0) s_evals = 0;
+  __shared__ unsigned long long s_evals, s_exact;
+  if (threadIdx.x == 0) { s_evals = 0; s_exact = 0; }
   __syncthreads();
   atomicAdd(&s_evals, (unsigned long long)my_evals);
+  atomicAdd(&s_exact, (unsigned long long)my_exact);
   __syncthreads();
-  if (threadIdx.x == 0) atomicAdd((unsigned long long *)&ctl->corner_evals, s_evals);
+  if (threadIdx.x == 0) {
+    atomicAdd((unsigned long long *)&ctl->corner_evals, s_evals);
+    atomicAdd((unsigned long long *)&ctl->exact_evals, s_exact);
+  }
   if (gtid == 0) {
     ctl->iterations = it;
     atomicAdd((unsigned long long *)&ctl->vertex_updates, (unsigned long long)my_updates);
@@ -497,13 +697,13 @@ __global__ void __launch_bounds__(256) fim_solve_kernel(FimDev d, FimParams p)
 
 cudaError_t launch_metric(const int32_t *tslots, const int64_t *cidx, const double *xyz,
                           const double *fib, const double *cf, const double *ct, int64_t nT,
-                          double *cgeo, cudaStream_t stream)
+                          double *cgeo, float *cgf, cudaStream_t stream)
 {
   if (nT <= 0) return cudaSuccess;
   const int block = 256;
   int64_t grid = (nT + block - 1) / block;
   if (grid > 152 * 64) grid = 152 * 64;
-  fim_metric_kernel<<<(unsigned)grid, block, 0, stream>>>(tslots, cidx, xyz, fib, cf, ct, nT, cgeo);
+  fim_metric_kernel<<<(unsigned)grid, block, 0, stream>>>(tslots, cidx, xyz, fib, cf, ct, nT, cgeo, cgf);
   return cudaGetLastError();
 }
 

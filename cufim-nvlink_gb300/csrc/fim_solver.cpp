@@ -64,7 +64,8 @@ void fimgb::set_last_error(const char *msg) { g_last_error = msg; }
 struct fim_solver {
   fim_opts opts{};
   int device = 0;
-  cudaStream_t stream = nullptr;
+  cudaStream_t own_stream = nullptr;  // created by fim_create
+  cudaStream_t stream = nullptr;      // working stream (own_stream unless fim_set_stream)
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   std::string err;
   int grid = 0, block = 256;
@@ -86,6 +87,7 @@ struct fim_solver {
   DevBuf<int64_t> cidx, cptr, nptr;
   DevBuf<int4> cids;
   DevBuf<double> cgeo;
+  DevBuf<float> cgf, phi_f;
   DevBuf<int32_t> nbr;
   DevBuf<double> fib, cf, ct;
   // state
@@ -162,13 +164,14 @@ extern "C" int fim_create(const fim_opts *opts, fim_solver **out)
   s->opts = o;
   s->device = o.device;
   if ((e = cudaSetDevice(s->device)) != cudaSuccess ||
-      (e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking)) != cudaSuccess ||
+      (e = cudaStreamCreateWithFlags(&s->own_stream, cudaStreamNonBlocking)) != cudaSuccess ||
       (e = cudaEventCreate(&s->ev0)) != cudaSuccess || (e = cudaEventCreate(&s->ev1)) != cudaSuccess ||
       (e = solve_grid_size(s->device, s->block, &s->grid)) != cudaSuccess || (e = s->ctl.alloc(1)) != cudaSuccess) {
     int rc = set_err(nullptr, FIM_ERR_CUDA, "fim_create: %s", cudaGetErrorString(e));
     fim_destroy(s);
     return rc;
   }
+  s->stream = s->own_stream;
   int coop = 0;
   cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, s->device);
   if (!coop) {
@@ -184,11 +187,22 @@ extern "C" int fim_destroy(fim_solver *s)
   if (!s) return FIM_OK;
   cudaSetDevice(s->device);
   if (s->stream) cudaStreamSynchronize(s->stream);
+  if (s->own_stream) cudaStreamSynchronize(s->own_stream);
   if (s->ev0) cudaEventDestroy(s->ev0);
   if (s->ev1) cudaEventDestroy(s->ev1);
-  if (s->stream) cudaStreamDestroy(s->stream);
+  if (s->own_stream) cudaStreamDestroy(s->own_stream);
+  s->own_stream = nullptr;
   s->stream = nullptr;
   delete s;  // DevBuf destructors free device memory
+  return FIM_OK;
+}
+
+extern "C" int fim_set_stream(fim_solver *s, void *stream)
+{
+  if (!s) return set_err(nullptr, FIM_ERR_INVALID_ARGUMENT, "fim_set_stream: solver is NULL");
+  CUDA_TRY(s, cudaSetDevice(s->device));
+  CUDA_TRY(s, cudaStreamSynchronize(s->stream));
+  s->stream = stream ? (cudaStream_t)stream : s->own_stream;
   return FIM_OK;
 }
 
@@ -390,12 +404,14 @@ extern "C" int fim_set_mesh(fim_solver *s, int64_t nV, const double *xyz, int64_
   CUDA_TRY(s, s->cptr.alloc(nL + 1));
   CUDA_TRY(s, s->cids.alloc(nC));
   CUDA_TRY(s, s->cgeo.alloc(10 * nC));
+  CUDA_TRY(s, s->cgf.alloc(12 * nC));
   CUDA_TRY(s, s->nptr.alloc(nL + 1));
   CUDA_TRY(s, s->nbr.alloc(nbr.size()));
   CUDA_TRY(s, s->fib.alloc(3 * nT));
   CUDA_TRY(s, s->cf.alloc(nT));
   CUDA_TRY(s, s->ct.alloc(nT));
   CUDA_TRY(s, s->phi.alloc(nL));
+  CUDA_TRY(s, s->phi_f.alloc(nL));
   CUDA_TRY(s, s->phi2.alloc(nL));
   CUDA_TRY(s, s->st.alloc(nL));
   CUDA_TRY(s, s->tst.alloc(nL));
@@ -435,7 +451,7 @@ extern "C" int fim_set_mesh(fim_solver *s, int64_t nV, const double *xyz, int64_
 static int run_metric(fim_solver *s)
 {
   CUDA_TRY(s, cudaEventRecord(s->ev0, s->stream));
-  CUDA_TRY(s, launch_metric(s->tslots.p, s->cidx.p, s->xyz.p, s->fib.p, s->cf.p, s->ct.p, s->nT, s->cgeo.p,
+  CUDA_TRY(s, launch_metric(s->tslots.p, s->cidx.p, s->xyz.p, s->fib.p, s->cf.p, s->ct.p, s->nT, s->cgeo.p, s->cgf.p,
                             s->stream));
   CUDA_TRY(s, cudaEventRecord(s->ev1, s->stream));
   CUDA_TRY(s, cudaEventSynchronize(s->ev1));
@@ -538,7 +554,8 @@ extern "C" int fim_solve(fim_solver *s, void *stream)
   FimDev d{};
   d.nV = (int32_t)s->nL; d.nG = (int32_t)s->nV; d.nT = s->nT; d.nC = s->nC;
   d.gptr = s->gptr.p; d.gcopy = s->gcopy.p; d.phi_out = s->phi_out.p; d.st_out = s->st_out.p;
-  d.cptr = s->cptr.p; d.cids = s->cids.p; d.cgeo = s->cgeo.p; d.nptr = s->nptr.p; d.nbr = s->nbr.p;
+  d.cptr = s->cptr.p; d.cids = s->cids.p; d.cgeo = s->cgeo.p; d.cgf = s->cgf.p; d.nptr = s->nptr.p; d.nbr = s->nbr.p;
+  d.phi_f = s->phi_f.p;
   d.phi = s->phi.p; d.phi2 = s->phi2.p; d.st = s->st.p; d.tst = s->tst.p; d.flag = s->flag.p;
   d.list[0] = s->list0.p; d.list[1] = s->list1.p; d.list[2] = s->list2.p;
   d.lfrozen = s->lfrozen.p; d.lmarked = s->lmarked.p; d.dec = s->dec.p;
@@ -553,6 +570,7 @@ extern "C" int fim_solve(fim_solver *s, void *stream)
   p.timeout_ns = (uint64_t)(s->opts.timeout_s * 1e9);
   p.withhold_block = (s->opts.test_withhold_block > 0 && s->opts.test_withhold_block <= s->grid)
                          ? s->opts.test_withhold_block : 0;
+  p.exact_all = s->opts.exact_all ? 1 : 0;
   CUDA_TRY(s, cudaMemsetAsync(s->ctl.p, 0, sizeof(FimCtl), st));
   CUDA_TRY(s, cudaEventRecord(s->ev0, st));
   CUDA_TRY(s, launch_solve(d, p, s->grid, s->block, st));
@@ -565,6 +583,7 @@ extern "C" int fim_solve(fim_solver *s, void *stream)
   s->stats.iterations = s->last_ctl.iterations;
   s->stats.vertex_updates = s->last_ctl.vertex_updates;
   s->stats.corner_evals = s->last_ctl.corner_evals;
+  s->stats.exact_evals = s->last_ctl.exact_evals;
   s->stats.grid_blocks = s->grid;
   s->stats.block_threads = s->block;
   if (s->last_ctl.error == KERR_TIMEOUT)

@@ -24,18 +24,18 @@ FAR, NEIG, NARROW, NEXT, FROZEN, TAIL = range(6)
 EXPORTS = ["fim_default_opts", "fim_create", "fim_destroy", "fim_last_error", "fim_set_mesh",
            "fim_set_conduction", "fim_set_conduction_device", "fim_set_stimuli", "fim_solve",
            "fim_get_times", "fim_get_times_device", "fim_get_stats", "fim_vtk_read", "fim_vtk_write",
-           "fim_read_tags", "fim_load_plan"]
+           "fim_read_tags", "fim_load_plan", "fim_set_stream"]
 
 
 class FimOpts(C.Structure):
     _fields_ = [("device", C.c_int), ("dt", C.c_double), ("n_steps", C.c_int), ("front_width", C.c_double),
                 ("apd", C.c_double), ("max_iterations", C.c_int64), ("timeout_s", C.c_double),
-                ("verbose", C.c_int), ("test_withhold_block", C.c_int)]
+                ("verbose", C.c_int), ("test_withhold_block", C.c_int), ("exact_all", C.c_int)]
 
 
 class FimStats(C.Structure):
     _fields_ = [("iterations", C.c_int64), ("vertex_updates", C.c_int64), ("corner_evals", C.c_int64),
-                ("solve_ms", C.c_double), ("metric_ms", C.c_double), ("n_corners", C.c_int64),
+                ("exact_evals", C.c_int64), ("solve_ms", C.c_double), ("metric_ms", C.c_double), ("n_corners", C.c_int64),
                 ("grid_blocks", C.c_int), ("block_threads", C.c_int)]
 
 
@@ -73,6 +73,7 @@ def lib():
         L.fim_set_conduction_device.argtypes = [vp, vp, vp, vp]
         L.fim_set_stimuli.argtypes = [vp, i64, P(i64), P(d)]
         L.fim_solve.argtypes = [vp, vp]
+        L.fim_set_stream.argtypes = [vp, vp]
         L.fim_get_times.argtypes = [vp, P(d), P(i32)]
         L.fim_get_times_device.argtypes = [vp, vp]
         L.fim_get_stats.argtypes = [vp, P(FimStats)]
@@ -158,6 +159,10 @@ class Solver:
 
     def solve(self, stream=None):
         _check(lib().fim_solve(self.h, C.c_void_p(stream) if stream else None), self.h)
+
+    def set_stream(self, stream):
+        """Working stream (an integer cudaStream_t, e.g. torch's stream.cuda_stream; 0/None = own)."""
+        _check(lib().fim_set_stream(self.h, C.c_void_p(stream) if stream else None), self.h)
 
     def times(self, with_state=True):
         phi = np.empty(self.nV, dtype=np.float64)

@@ -66,6 +66,9 @@ typedef struct {
                               skip its first grid-barrier arrival, so the other
                               blocks' bounded waits expire and fim_solve returns
                               FIM_ERR_TIMEOUT; 0 = off                             */
+  int exact_all;         /* 1: solve every triangle/tet candidate in FP64 instead of
+                              screening them with FP32 interval bounds first; the
+                              results are identical, only slower (cross-check)     */
 } fim_opts;
 
 /* Defaults: device 0, one endless window, reference front width, APD off. */
@@ -99,9 +102,13 @@ int fim_set_conduction_device(fim_solver *s, const double *d_fib, const double *
  * stimulus at time 0, update_events_gpu, cuda_fim.cu:632-683). */
 int fim_set_stimuli(fim_solver *s, int64_t n, const int64_t *vertices, const double *t0);
 
-/* Runs the solve on `stream` (a cudaStream_t, NULL = the solver's own
+/* Runs the solve on `stream` (a cudaStream_t, NULL = the solver's working
  * stream) and waits for it. */
 int fim_solve(fim_solver *s, void *stream);
+
+/* Sets the working stream (a cudaStream_t on the solver's device) of all
+ * later transfers and launches of this solver; NULL restores its own. */
+int fim_set_stream(fim_solver *s, void *stream);
 
 /* Results of the last solve: phi[n_vertices] (FP64; the reference's INF,
  * DBL_MAX, for unreached vertices) and state[n_vertices] (or NULL). */
@@ -112,7 +119,8 @@ int fim_get_times_device(fim_solver *s, double *d_phi);
 typedef struct {
   int64_t iterations;      /* FIM iterations (all windows)                  */
   int64_t vertex_updates;  /* vertex solves (narrow + re-solved neighbours) */
-  int64_t corner_evals;    /* (vertex, tet) local solves evaluated          */
+  int64_t corner_evals;    /* (vertex, tet) corners screened                */
+  int64_t exact_evals;     /* triangle/tet solves done in FP64              */
   double solve_ms;         /* device time of the last fim_solve             */
   double metric_ms;        /* device time of the last metric precompute     */
   int64_t n_corners;       /* (vertex, tet) pairs of the mesh               */

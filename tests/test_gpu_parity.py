@@ -233,3 +233,44 @@ def test_device_resident_inputs_and_outputs(F, O):
     torch.cuda.synchronize()
     phi_o, _, _, _ = oracle_single(O, c)
     assert np.array_equal(out.cpu().numpy(), phi_o)
+
+
+@pytest.mark.parametrize("exact_all", [0, 1])
+def test_filtered_and_exact_paths_agree(F, O, exact_all):
+    """The interval-screened path and the all-FP64 path both equal the oracle."""
+    import fim_mesh
+    c = fim_mesh.slab_case(cells=(30, 12, 6), size=(20.0, 7.0, 3.0), seed=8)
+    phi, st, stats = F.solve_case(c, exact_all=exact_all)
+    phi_o, st_o, _, _ = oracle_single(O, c)
+    assert_identical(phi, st, phi_o, st_o)
+    if exact_all:
+        assert stats["exact_evals"] > 0
+
+
+@pytest.mark.parametrize("scale", [1e-3, 1.0, 1e3, 1e5])
+def test_unit_scales_bit_exact(F, O, scale):
+    """The reference's tet solve is not scale invariant; the filters must
+    stay exact in mm, um and larger units (the reference's files are um)."""
+    import fim_mesh
+    c = fim_mesh.slab_case(cells=(16, 8, 5), size=(4.0, 2.0, 1.25), scar_radius=0.5, seed=10)
+    c = dict(c, xyz=c["xyz"] * scale, seed_t=c["seed_t"] * scale)
+    phi, st, _ = F.solve_case(c)
+    phi_o, st_o, _, _ = oracle_single(O, c)
+    assert_identical(phi, st, phi_o, st_o)
+
+
+def test_random_metrics_bit_exact(F, O):
+    """Strongly anisotropic random fibres and speeds per tet."""
+    import fim_mesh
+    xyz, tets = fim_mesh.kuhn_box(14, 10, 8, 3.5, 2.5, 2.0, jitter=0.25, seed=21)
+    nT = tets.shape[0]
+    rng = np.random.default_rng(5)
+    f = rng.normal(size=(nT, 3))
+    f /= np.linalg.norm(f, axis=1, keepdims=True)
+    cf = rng.uniform(0.2, 1.5, nT)
+    ct = cf * rng.uniform(0.1, 1.0, nT)
+    c = dict(xyz=xyz, tets=tets, fib=f, cf=cf, ct=ct, seed_v=np.array([0, 500, 1000]),
+             seed_t=np.array([0.0, 0.3, 0.1]))
+    phi, st, _ = F.solve_case(c)
+    phi_o, st_o, _, _ = oracle_single(O, c)
+    assert_identical(phi, st, phi_o, st_o)
