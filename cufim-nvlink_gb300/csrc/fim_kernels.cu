@@ -286,152 +286,114 @@ __device__ __forceinline__ double dunkey(unsigned long long k)
   return __longlong_as_double((long long)b);
 }
 
-constexpr int kWarps = 8;            // warps per block (256 threads)
-constexpr int kMaxVpw = 8;           // vertices per warp per batch
-constexpr int kSlots = kWarps * kMaxVpw;
-constexpr int kQcap = 1024;          // exact solves queued per kind and batch
+constexpr int kThreads = 256;       // threads per block of the solve kernel
+constexpr int kSlots = 32;          // vertices per batch (at most)
+constexpr int kCornerCap = 768;     // corners per batch
+constexpr int kTriCap = 1024;       // triangle screens per batch (more are screened on the spot)
+constexpr int kTetCap = 768;        // tet screens per batch
+constexpr int kQcap = 512;          // exact solves queued per kind and batch
+
+// Order-preserving map of floats to unsigned integers (for atomicMin).
+__device__ __forceinline__ unsigned int fkey(float x)
+{
+  const unsigned int b = __float_as_uint(x);
+  return (b >> 31) ? ~b : (b | 0x80000000u);
+}
+__device__ __forceinline__ float funkey(unsigned int k)
+{
+  return __uint_as_float((k >> 31) ? (k & 0x7fffffffu) : ~k);
+}
 
 // Shared memory of one batch of vertex updates.
 struct BatchSh {
   int32_t vtx[kSlots];
   int64_t c0[kSlots];
+  int32_t cp[kSlots + 1];           // corner prefix over the batch's vertices
   double old[kSlots];
-  unsigned long long res[kSlots];  // dkey of the running minimum
-  uint32_t q[2][kQcap];            // queued exact solves: [0] tets, [1] triangles
-  int nq[2];
+  unsigned long long res[kSlots];   // dkey of the running minimum (exact values)
+  unsigned int bhi[kSlots];         // fkey of a float upper bound of the new time
+  // per corner of the batch: float times of the other three vertices,
+  // float edge lengths, validity bits
+  float pf[kCornerCap][3];
+  float sf[kCornerCap][3];
+  uint8_t vm[kCornerCap];
+  // compacted screen lists: item (corner j | pair k << 16) and lower bound
+  uint32_t tri[kTriCap];
+  float tri_lb[kTriCap];
+  uint32_t tet[kTetCap];
+  float tet_lb[kTetCap];
+  uint32_t q[2][kQcap];             // queued exact solves: [0] tets, [1] triangles
+  int ntri, ntet, nq[2];
+  int nslot;                        // vertices of the current batch
 };
 
-// Queue item: slot (6 bits) | kind (2 bits) | corner offset in the vertex (24 bits).
+// Queue item: slot (5 bits) | kind (2 bits) | corner offset in the vertex (25 bits).
 __device__ __forceinline__ uint32_t make_item(int slot, int kind, int64_t off)
 {
-  return (uint32_t)slot | ((uint32_t)kind << 6) | ((uint32_t)off << 8);
+  return (uint32_t)slot | ((uint32_t)kind << 5) | ((uint32_t)off << 7);
 }
 
-// Screens all corners of vertex v (one warp, lanes over corners).  First
-// pass: float bounds of the edge candidates give an upper bound bhi of the
-// vertex's new time; the edge candidates that can still be the minimum are
-// added exactly (one FP64 add each).  Second pass: triangle and tet solves
-// whose trivial bound min(neighbour times) is below bhi are screened
-// (fim_filter.cuh); those that can still be the minimum are queued for the
-// exact FP64 solve.  The minimum of everything equals the reference's
-// update_per_element minimum over all corners (cuda_fim.h:1362-1411), with
-// the validity rule state >= narrow and phi > phi_start - front_width; the
-// rule is decided on the float copies when they are conclusive and on the
-// FP64 times otherwise.
-__device__ void warp_filter_vertex(const FimDev &d, BatchSh &sh, int slot, int32_t v, double lower,
-                                   float lower_lo, float lower_hi, bool exact_all, int lane, int64_t &n_filtered)
+__device__ __forceinline__ int slot_of(const BatchSh &sh, int nslot, int j)
 {
-  const double old = __ldcg(d.phi + v);
-  const int64_t c0 = d.cptr[v], c1 = d.cptr[v + 1];
-  if (lane == 0) { sh.vtx[slot] = v; sh.c0[slot] = c0; sh.old[slot] = old; sh.res[slot] = dkey(old); }
-  float bhi = exact_all ? INFINITY : re_hi(re_in(__ldcg(d.phi_f + v)));
-  for (int64_t cc = c0; cc < c1; cc += 32) {
-    const int64_t c = cc + lane;
-    bool vv[3] = {false, false, false};
-    Re P[3];
-    float4 r0 = make_float4(0.f, 0.f, 0.f, 0.f), r1 = r0, r2 = r0;
-    int4 id = make_int4(0, 0, 0, 0);
-    float lbE[3] = {INFINITY, INFINITY, INFINITY};
-    float ub = INFINITY;
-    if (c < c1) {
-      id = __ldg(d.cids + c);
-      const int32_t nb[3] = {id.x, id.y, id.z};
-#pragma unroll
-      for (int i = 0; i < 3; ++i) {
-        const float pf = __ldcg(d.phi_f + nb[i]);
-        P[i] = re_in(pf);
-        bool ok = __ldcg(d.st + nb[i]) >= ST_NARROW;
-        if (ok) {
-          if (re_lo(P[i]) > lower_hi) ok = true;
-          else if (re_hi(P[i]) <= lower_lo) ok = false;
-          else ok = __ldcg(d.phi + nb[i]) > lower;
-        }
-        vv[i] = ok;
-      }
-      if (vv[0] || vv[1] || vv[2]) {
-        ++n_filtered;
-        const float4 *rp = reinterpret_cast<const float4 *>(d.cgf + 12 * c);
-        r0 = __ldg(rp);
-        r1 = __ldg(rp + 1);
-        r2 = __ldg(rp + 2);
-        const float sv[3] = {r1.z, r1.w, r2.x};
-#pragma unroll
-        for (int i = 0; i < 3; ++i)
-          if (vv[i]) {
-            const Re E = P[i] + re_in(sv[i]);
-            lbE[i] = re_lo(E);
-            ub = fminf(ub, re_hi(E));
-          }
-      }
-    }
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) ub = fminf(ub, __shfl_xor_sync(FULL_MASK, ub, off));
-    if (!exact_all) bhi = fminf(bhi, ub);
-    // exact edge candidates that can still be the minimum
-    if (c < c1) {
-      const int32_t nb[3] = {id.x, id.y, id.z};
-#pragma unroll
-      for (int i = 0; i < 3; ++i)
-        if (vv[i] && !(lbE[i] > bhi)) {
-          const double val = __ldcg(d.phi + nb[i]) + __ldg(d.cgeo + 10 * c + 6 + i);
-          atomicMin(&sh.res[slot], dkey(val));
-        }
-    }
-    // triangle and tet screens
-    CandBound cb[4];
-#pragma unroll
-    for (int k = 0; k < 4; ++k) { cb[k].some = CAND_NONE; cb[k].lb = NAN; cb[k].ub = INFINITY; }
-    float ub2 = INFINITY;
-    if (c < c1 && (vv[0] || vv[1] || vv[2])) {
-      const bool bad = exact_all || r2.z != 0.f;
-      const int ks = (int)r2.y;
-      const float tk = re_pow2f(ks);
-      const Re gs[6] = {re_in(r0.x), re_in(r0.y), re_in(r0.z), re_in(r0.w), re_in(r1.x), re_in(r1.y)};
-      const float lo0 = re_lo(P[0]), lo1 = re_lo(P[1]), lo2 = re_lo(P[2]);
-      // pairs (1,2), (2,3), (1,3): kind 0, 1, 2
-      if (vv[0] && vv[1] && !(fminf(lo0, lo1) > bhi)) {
-        if (bad) cb[0].some = CAND_SOME;
-        else cb[0] = tri_screen(re_scale(gs[3], tk), re_scale(gs[4], tk), re_scale(gs[5], tk), P[0], P[1]);
-      }
-      if (vv[1] && vv[2] && !(fminf(lo1, lo2) > bhi)) {
-        if (bad) cb[1].some = CAND_SOME;
-        else cb[1] = tri_screen(re_scale(gs[1], tk), re_scale(gs[5], tk), re_scale(gs[2], tk), P[1], P[2]);
-      }
-      if (vv[0] && vv[2] && !(fminf(lo0, lo2) > bhi)) {
-        if (bad) cb[2].some = CAND_SOME;
-        else cb[2] = tri_screen(re_scale(gs[0], tk), re_scale(gs[4], tk), re_scale(gs[2], tk), P[0], P[2]);
-      }
-      if (vv[0] && vv[1] && vv[2] && !(fminf(lo0, fminf(lo1, lo2)) > bhi)) {
-        if (bad) cb[3].some = CAND_SOME;
-        else cb[3] = tet_screen(gs, P[0], P[1], P[2], ks);
-      }
-#pragma unroll
-      for (int k = 0; k < 4; ++k)
-        if (cb[k].some) ub2 = fminf(ub2, cb[k].ub);
-    }
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) ub2 = fminf(ub2, __shfl_xor_sync(FULL_MASK, ub2, off));
-    if (!exact_all) bhi = fminf(bhi, ub2);
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      const bool need = cb[k].some && !(cb[k].lb > bhi);
-      const unsigned mask = __ballot_sync(FULL_MASK, need);
-      if (mask == 0) continue;
-      const int qi = (k == 3) ? 0 : 1;
-      int base = 0;
-      if (lane == 0) base = atomicAdd(&sh.nq[qi], __popc(mask));
-      base = __shfl_sync(FULL_MASK, base, 0);
-      if (need) {
-        const int pos = base + __popc(mask & ((1u << lane) - 1u));
-        if (pos < kQcap) {
-          sh.q[qi][pos] = make_item(slot, k, c - c0);
-        } else {  // queue full: solve here
-          const double val = exact_candidate(d, c, k);
-          if (val < FIM_INF) atomicMin(&sh.res[slot], dkey(val));
-        }
-      }
-    }
+  int lo = 0, hi = nslot - 1;  // last slot with cp[slot] <= j
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (sh.cp[mid] <= j) lo = mid; else hi = mid - 1;
   }
+  return lo;
+}
+
+// Appends one item per lane with `need` to a list in shared memory
+// (warp-ballot compaction).  Returns the item's position, or -1.
+__device__ __forceinline__ int warp_append(int *counter, bool need, int lane)
+{
+  const unsigned mask = __ballot_sync(FULL_MASK, need);
+  if (mask == 0) return -1;
+  int base = 0;
+  if (lane == 0) base = atomicAdd(counter, __popc(mask));
+  base = __shfl_sync(FULL_MASK, base, 0);
+  return need ? base + __popc(mask & ((1u << lane) - 1u)) : -1;
+}
+
+// Queues an exact solve (or runs it on the spot when the queue is full).
+// qi (0: tets, 1: triangles) must be the same on every lane of the warp; the
+// item's kind may differ per lane.
+__device__ __forceinline__ void queue_exact(const FimDev &d, BatchSh &sh, bool need, int qi, int kind, int slot,
+                                            int64_t c, int lane)
+{
+  const int pos = warp_append(&sh.nq[qi], need, lane);
+  if (pos < 0) return;
+  if (pos < kQcap) {
+    sh.q[qi][pos] = make_item(slot, kind, c - sh.c0[slot]);
+  } else {
+    const double val = exact_candidate(d, c, kind);
+    if (val < FIM_INF) atomicMin(&sh.res[slot], dkey(val));
+  }
+}
+
+// Triangle screen of pair k (0: (1,2), 1: (2,3), 2: (1,3)) of corner c.
+__device__ __forceinline__ CandBound tri_screen_of(const FimDev &d, int64_t c, int k, const float *pf)
+{
+  const float4 *rp = reinterpret_cast<const float4 *>(d.cgf + 12 * c);
+  const float4 r0 = __ldg(rp), r1 = __ldg(rp + 1), r2 = __ldg(rp + 2);
+  const float tk = re_pow2f((int)r2.y);
+  // scaled e13, e23, e34, e12, e14, e24 -> true units
+  const float g[6] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y};
+  const int i12 = k == 0 ? 3 : (k == 1 ? 1 : 0);   // e12 role
+  const int i13 = k == 0 ? 4 : (k == 1 ? 5 : 4);   // e13 role
+  const int i23 = k == 0 ? 5 : 2;                  // e23 role
+  const int a = k == 0 ? 0 : (k == 1 ? 1 : 0), b = k == 0 ? 1 : 2;
+  return tri_screen(re_scale(re_in(g[i12]), tk), re_scale(re_in(g[i13]), tk), re_scale(re_in(g[i23]), tk),
+                    re_in(pf[a]), re_in(pf[b]));
+}
+
+// Tet screen of corner c.
+__device__ __forceinline__ CandBound tet_screen_of(const FimDev &d, int64_t c, const float *pf)
+{
+  const float4 *rp = reinterpret_cast<const float4 *>(d.cgf + 12 * c);
+  const float4 r0 = __ldg(rp), r1 = __ldg(rp + 1), r2 = __ldg(rp + 2);
+  const Re gs[6] = {re_in(r0.x), re_in(r0.y), re_in(r0.z), re_in(r0.w), re_in(r1.x), re_in(r1.y)};
+  return tet_screen(gs, re_in(pf[0]), re_in(pf[1]), re_in(pf[2]), (int)r2.y);
 }
 
 // Writes a time and its float copy.
@@ -441,55 +403,259 @@ __device__ __forceinline__ void set_phi(const FimDev &d, int64_t v, double x)
   d.phi_f[v] = (float)x;
 }
 
-// Solves the queued exact candidates of the batch with all threads of the
-// block (tets first, then triangles, each loop uniform in its work).
-__device__ void block_drain(const FimDev &d, BatchSh &sh, int64_t &n_exact)
-{
-#pragma unroll 1
-  for (int qi = 0; qi < 2; ++qi) {
-    const int n = min(sh.nq[qi], kQcap);
-    for (int j = threadIdx.x; j < n; j += blockDim.x) {
-      const uint32_t it = sh.q[qi][j];
-      const int slot = it & 63, kind = (it >> 6) & 3;
-      const int64_t c = sh.c0[slot] + (int64_t)(it >> 8);
-      const double val = exact_candidate(d, c, kind);
-      ++n_exact;
-      if (val < FIM_INF) atomicMin(&sh.res[slot], dkey(val));
-    }
-  }
-}
-
-// One update phase over a vertex list, processed in block batches: every
-// warp filters its vertices, the block then solves the queued exact
-// candidates of the whole batch with full warps, and finally applies the
-// reference's per-vertex decision.
-//  mode 0 -- narrow vertices: reduce per vertex, window test (next), freeze
-//            test (cuda_fim.cu:2125-2163);
-//  mode 1 -- re-solved neighbours: reduce and keep the decided state
-//            (cuda_fim.cu:2255-2289).
+// One update phase over a vertex list.  Every block takes a contiguous part
+// of the list and processes it in batches of up to kSlots vertices / up to
+// kCornerCap corners, the corners of a batch spread over all threads:
+//  A -- load every corner: validity of the neighbours (state >= narrow and
+//       phi > phi_start - front_width, on the float copies when conclusive,
+//       else on the FP64 times), float edge bounds -> per-vertex upper bound
+//       bhi of the new time;
+//  B -- exact FP64 edge candidates that can still be the minimum; triangle
+//       and tet solves whose trivial bound min(neighbour times) <= bhi are
+//       appended to compacted screen lists (warp-ballot compaction);
+//  S -- the screens run over the lists with full warps (triangles and tets
+//       on separate warps); certain upper bounds tighten bhi;
+//  C -- solves whose lower bound does not exceed bhi are queued;
+//  D -- the queued solves run in FP64 (tets and triangles on separate warps);
+//  E -- the reference's per-vertex decision on the exact minimum:
+//   mode 0 -- narrow vertices: window test (next), freeze test
+//             (cuda_fim.cu:2125-2163);
+//   mode 1 -- re-solved neighbours: keep or restore the state
+//             (cuda_fim.cu:2255-2289).
+// The minimum over everything equals the reference's update_per_element
+// minimum over all corners (cuda_fim.h:1362-1411).
 __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, int32_t n, int mode, double lower,
                              float lower_lo, float lower_hi, double phi_start, double dt, bool exact_all, int s,
                              int64_t &n_filtered, int64_t &n_exact)
 {
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t total_warps = (int64_t)gridDim.x * kWarps;
-  int vpw = (int)((n + total_warps - 1) / total_warps);
-  vpw = max(1, min(kMaxVpw, vpw));
-  const int nb = kWarps * vpw;
-  for (int64_t base = (int64_t)blockIdx.x * nb; base < n; base += (int64_t)gridDim.x * nb) {
-    if (threadIdx.x == 0) { sh.nq[0] = 0; sh.nq[1] = 0; }
-    __syncthreads();
-    const int nslot = (int)min((int64_t)nb, (int64_t)n - base);
-    for (int j = 0; j < vpw; ++j) {
-      const int slot = warp * vpw + j;
-      if (slot < nslot)
-        warp_filter_vertex(d, sh, slot, __ldcg(list + base + slot), lower, lower_lo, lower_hi, exact_all, lane,
-                           n_filtered);
+  const int tid = threadIdx.x, lane = tid & 31;
+  const int64_t per_block = ((int64_t)n + gridDim.x - 1) / gridDim.x;
+  const int64_t lbeg = min((int64_t)n, (int64_t)blockIdx.x * per_block);
+  const int64_t lend = min((int64_t)n, lbeg + per_block);
+  int64_t pos = lbeg;
+  while (pos < lend) {
+    // batch: the longest run of vertices with <= kCornerCap corners (>= 1 vertex)
+    const int cand = (int)min((int64_t)kSlots, lend - pos);
+    if (tid < cand) {
+      const int32_t v = __ldcg(list + pos + tid);
+      const double old = __ldcg(d.phi + v);
+      sh.vtx[tid] = v;
+      sh.c0[tid] = d.cptr[v];
+      sh.cp[tid + 1] = (int32_t)(d.cptr[v + 1] - d.cptr[v]);
+      sh.old[tid] = old;
+      sh.res[tid] = dkey(old);
+      sh.bhi[tid] = fkey(exact_all ? INFINITY : re_hi(re_in(__ldcg(d.phi_f + v))));
+    }
+    if (tid == 0) {
+      sh.cp[0] = 0;
+      sh.ntri = 0; sh.ntet = 0; sh.nq[0] = 0; sh.nq[1] = 0;
     }
     __syncthreads();
-    block_drain(d, sh, n_exact);
+    if (tid == 0) {
+      int k = 1;
+      for (; k <= cand; ++k) {
+        const int t = sh.cp[k - 1] + sh.cp[k];
+        if (t > kCornerCap && k > 1) break;
+        sh.cp[k] = t;
+      }
+      sh.nslot = k - 1;
+    }
     __syncthreads();
-    for (int slot = threadIdx.x; slot < nslot; slot += blockDim.x) {
+    const int nslot = sh.nslot;
+    const int total = sh.cp[nslot];     // may exceed kCornerCap for a single huge vertex
+    const int kept = min(total, kCornerCap);
+
+    // A: load, validity, float edge bounds
+    for (int j = tid; j < total; j += kThreads) {
+      const int slot = slot_of(sh, nslot, j);
+      const int64_t c = sh.c0[slot] + (j - sh.cp[slot]);
+      const int4 id = __ldg(d.cids + c);
+      const int32_t nb[3] = {id.x, id.y, id.z};
+      const float4 *rp = reinterpret_cast<const float4 *>(d.cgf + 12 * c);
+      const float4 r1 = __ldg(rp + 1), r2 = __ldg(rp + 2);
+      const float sv[3] = {r1.z, r1.w, r2.x};
+      uint32_t m = 0;
+      float pf[3];
+      float ub = INFINITY;
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        pf[i] = __ldcg(d.phi_f + nb[i]);
+        const Re P = re_in(pf[i]);
+        bool ok = __ldcg(d.st + nb[i]) >= ST_NARROW;
+        if (ok) {
+          if (re_lo(P) > lower_hi) ok = true;
+          else if (re_hi(P) <= lower_lo) ok = false;
+          else ok = __ldcg(d.phi + nb[i]) > lower;
+        }
+        if (ok) {
+          m |= 1u << i;
+          ub = fminf(ub, re_hi(P + re_in(sv[i])));
+        }
+      }
+      if (m) ++n_filtered;
+      if (!exact_all && ub < INFINITY) atomicMin(&sh.bhi[slot], fkey(ub));
+      if (j < kCornerCap) {
+        sh.vm[j] = (uint8_t)m;
+#pragma unroll
+        for (int i = 0; i < 3; ++i) { sh.pf[j][i] = pf[i]; sh.sf[j][i] = sv[i]; }
+      }
+    }
+    __syncthreads();
+
+    // B: exact edges; screen lists
+    for (int jb = 0; jb < kept; jb += kThreads) {
+      const int j = jb + tid;
+      const bool in = j < kept;
+      int slot = 0;
+      int64_t c = 0;
+      uint32_t m = 0;
+      float bhi = 0.f, lo[3] = {0.f, 0.f, 0.f};
+      if (in) {
+        slot = slot_of(sh, nslot, j);
+        c = sh.c0[slot] + (j - sh.cp[slot]);
+        m = sh.vm[j];
+        bhi = funkey(sh.bhi[slot]);
+        const int4 id = __ldg(d.cids + c);
+        const int32_t nb[3] = {id.x, id.y, id.z};
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+          const Re P = re_in(sh.pf[j][i]);
+          lo[i] = re_lo(P);
+          if ((m >> i) & 1u) {
+            if (!(re_lo(P + re_in(sh.sf[j][i])) > bhi)) {
+              const double val = __ldcg(d.phi + nb[i]) + __ldg(d.cgeo + 10 * c + 6 + i);
+              atomicMin(&sh.res[slot], dkey(val));
+            }
+          }
+        }
+      }
+      // triangle pairs (1,2), (2,3), (1,3) and the tet
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const int a = k == 1 ? 1 : 0, b = k == 0 ? 1 : 2;
+        const bool need = in && ((m >> a) & 1u) && ((m >> b) & 1u) && !(fminf(lo[a], lo[b]) > bhi);
+        const int p = warp_append(&sh.ntri, need, lane);
+        if (p >= 0) {
+          if (p < kTriCap) {
+            sh.tri[p] = (uint32_t)j | ((uint32_t)k << 16);
+          } else {  // list full: screen here
+            CandBound cb;
+            if (exact_all) { cb.some = CAND_SOME; cb.lb = NAN; cb.ub = INFINITY; }
+            else cb = tri_screen_of(d, c, k, sh.pf[j]);
+            if (cb.some && !(cb.lb > bhi)) {
+              const double val = exact_candidate(d, c, k);
+              if (val < FIM_INF) atomicMin(&sh.res[slot], dkey(val));
+            }
+          }
+        }
+      }
+      {
+        const bool need = in && m == 7u && !(fminf(lo[0], fminf(lo[1], lo[2])) > bhi);
+        const int p = warp_append(&sh.ntet, need, lane);
+        if (p >= 0) sh.tet[p] = (uint32_t)j;  // kTetCap == kCornerCap: never full
+      }
+    }
+    // corners beyond kCornerCap (a single vertex with very many corners):
+    // every solve of them goes to FP64
+    for (int jb = kept; jb < total; jb += kThreads) {
+      const int j = jb + tid;
+      if (j >= total) continue;
+      const int slot = slot_of(sh, nslot, j);
+      const int64_t c = sh.c0[slot] + (j - sh.cp[slot]);
+      const int4 id = __ldg(d.cids + c);
+      const int32_t nb[3] = {id.x, id.y, id.z};
+      uint32_t m = 0;
+      for (int i = 0; i < 3; ++i) {
+        const double p = __ldcg(d.phi + nb[i]);
+        if (__ldcg(d.st + nb[i]) >= ST_NARROW && p > lower) {
+          m |= 1u << i;
+          atomicMin(&sh.res[slot], dkey(p + __ldg(d.cgeo + 10 * c + 6 + i)));
+        }
+      }
+      for (int k = 0; k < 4; ++k) {
+        const bool use = k == 3 ? m == 7u : (((m >> (k == 1 ? 1 : 0)) & 1u) && ((m >> (k == 0 ? 1 : 2)) & 1u));
+        if (!use) continue;
+        const double val = exact_candidate(d, c, k);
+        if (val < FIM_INF) atomicMin(&sh.res[slot], dkey(val));
+      }
+    }
+    __syncthreads();
+
+    // S: screens over the compacted lists; tets from thread 0, triangles from
+    // the next warp boundary
+    {
+      const int ntet = min(sh.ntet, kTetCap), ntri = min(sh.ntri, kTriCap);
+      const int tri0 = (ntet + 31) & ~31;
+      for (int i = tid; i < tri0 + ntri; i += kThreads) {
+        if (i < ntet) {
+          const int j = (int)sh.tet[i];
+          const int slot = slot_of(sh, nslot, j);
+          const int64_t c = sh.c0[slot] + (j - sh.cp[slot]);
+          CandBound cb;
+          if (exact_all) { cb.some = CAND_SOME; cb.lb = NAN; cb.ub = INFINITY; }
+          else cb = tet_screen_of(d, c, sh.pf[j]);
+          sh.tet_lb[i] = !cb.some ? NAN : (isnan(cb.lb) ? -INFINITY : cb.lb);
+          if (!exact_all && cb.some && cb.ub < INFINITY) atomicMin(&sh.bhi[slot], fkey(cb.ub));
+        } else if (i >= tri0) {
+          const int t = i - tri0;
+          const int j = (int)(sh.tri[t] & 0xffffu), k = (int)(sh.tri[t] >> 16);
+          const int slot = slot_of(sh, nslot, j);
+          const int64_t c = sh.c0[slot] + (j - sh.cp[slot]);
+          CandBound cb;
+          if (exact_all) { cb.some = CAND_SOME; cb.lb = NAN; cb.ub = INFINITY; }
+          else cb = tri_screen_of(d, c, k, sh.pf[j]);
+          sh.tri_lb[t] = !cb.some ? NAN : (isnan(cb.lb) ? -INFINITY : cb.lb);
+          if (!exact_all && cb.some && cb.ub < INFINITY) atomicMin(&sh.bhi[slot], fkey(cb.ub));
+        }
+      }
+    }
+    __syncthreads();
+
+    // C: queue the solves that can still be the minimum
+    {
+      const int ntet = min(sh.ntet, kTetCap), ntri = min(sh.ntri, kTriCap);
+      for (int ib = 0; ib < ntet + ntri; ib += kThreads) {
+        const int i = ib + tid;
+        bool need = false;
+        int kind = 0, slot = 0;
+        int64_t c = 0;
+        if (i < ntet + ntri) {
+          int j;
+          float l;
+          if (i < ntet) { j = (int)sh.tet[i]; kind = 3; l = sh.tet_lb[i]; }
+          else { const uint32_t it = sh.tri[i - ntet]; j = (int)(it & 0xffffu); kind = (int)(it >> 16); l = sh.tri_lb[i - ntet]; }
+          slot = slot_of(sh, nslot, j);
+          c = sh.c0[slot] + (j - sh.cp[slot]);
+          need = l <= funkey(sh.bhi[slot]);  // NaN (no value) never
+        }
+        // separate ballots per queue keep each queue warp-compacted
+        queue_exact(d, sh, need && kind == 3, 0, kind, slot, c, lane);
+        queue_exact(d, sh, need && kind != 3, 1, kind, slot, c, lane);
+      }
+    }
+    __syncthreads();
+
+    // D: exact solves; tets from thread 0, triangles from the next warp boundary
+    {
+      const int ntet = min(sh.nq[0], kQcap), ntri = min(sh.nq[1], kQcap);
+      const int tri0 = (ntet + 31) & ~31;
+      for (int j = tid; j < tri0 + ntri; j += kThreads) {
+        uint32_t it;
+        if (j < ntet) it = sh.q[0][j];
+        else if (j >= tri0) it = sh.q[1][j - tri0];
+        else continue;
+        const int slot = it & 31, kind = (it >> 5) & 3;
+        const int64_t c = sh.c0[slot] + (int64_t)(it >> 7);
+        const double val = exact_candidate(d, c, kind);
+        ++n_exact;
+        if (val < FIM_INF) atomicMin(&sh.res[slot], dkey(val));
+      }
+    }
+    __syncthreads();
+
+    // E: decisions
+    if (tid < nslot) {
+      const int slot = tid;
       const int32_t v = sh.vtx[slot];
       const double old = sh.old[slot];
       const double nw = dunkey(sh.res[slot]);
@@ -503,10 +669,11 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
           d.lfrozen[atomicAdd(&d.ctl->n_frozen[s], 1)] = v;
         }
       } else {
-        d.dec[base + slot] = (nw < old) ? (uint8_t)ST_NARROW : __ldcg(d.tst + v);
+        d.dec[pos + slot] = (nw < old) ? (uint8_t)ST_NARROW : __ldcg(d.tst + v);
       }
     }
     __syncthreads();
+    pos += nslot;
   }
 }
 
