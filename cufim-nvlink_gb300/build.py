@@ -4,7 +4,7 @@ Outputs (under cufim-nvlink_gb300/_build/):
   * libfim_gb300.so -- the C ABI of include/fim.h (kernels + host staging + I/O)
   * fim_cli         -- the reference-compatible command line front end
 
-The CUDA translation unit is compiled with -fmad=false: the solver's FP64
+The CUDA translation units are compiled with -fmad=false: the solver's FP64
 arithmetic must follow the reference's source operation by operation.
 """
 import concurrent.futures as cf
@@ -20,7 +20,7 @@ CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SOURCES = ["fim_kernels.cu"]
+CU_SOURCES = ["fim_kernels.cu", "fim_static.cu"]
 CPP_SOURCES = ["fim_solver.cpp", "fim_io.cpp", "cuda_solver_fim.cpp"]
 CLI_SOURCES = ["fim_cli.cpp"]
 

@@ -99,4 +99,30 @@ cudaError_t solve_grid_size(int device, int block, int *grid);
 // Writes phi (any order) into out.
 cudaError_t launch_copy(const double *src, double *dst, int64_t n, cudaStream_t stream);
 
+// ---- fixed scratch of fim_solve_noalloc (fim_static.cu) ----
+constexpr int64_t kStaticMaxCopies = 131072;       // vertex copies of the mesh
+constexpr int64_t kStaticMaxVertices = 131072;     // mesh vertices
+constexpr int64_t kStaticMaxSeeds = 8192;          // stimulus entries as given
+constexpr int64_t kStaticMaxSeedEntries = 32768;   // stimulus entries expanded to vertex copies
+
+// Pointers into the fixed scratch of one device.
+struct NoallocScratch {
+  double *phi, *phi2;
+  int32_t *flag, *list[3], *lfrozen, *lmarked;
+  float *phi_f;
+  uint8_t *st, *tst, *dec, *st_out;
+  unsigned long long *key;   // per mesh vertex: earliest stimulus time (order-preserving key)
+  int64_t *raw_v;            // stimuli as given
+  double *raw_t;
+  int32_t *seed_v;           // stimuli expanded to vertex copies
+  double *seed_t;
+  FimCtl *ctl;
+};
+// Resolves the scratch address on `device` (must be the current device); the
+// first call per device does the lookup, later calls reuse it.
+cudaError_t noalloc_scratch(int device, NoallocScratch *out);
+// Expands sc.raw_v/raw_t[n] into sc.seed_v/seed_t (one block).
+cudaError_t launch_noalloc_seeds(const NoallocScratch &sc, int32_t n, const int64_t *gptr,
+                                 const int32_t *gcopy, const int64_t *cptr, cudaStream_t stream);
+
 }  // namespace fimgb

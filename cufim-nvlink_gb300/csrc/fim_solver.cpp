@@ -632,3 +632,91 @@ extern "C" int fim_get_stats(const fim_solver *s, fim_stats *out)
   *out = s->stats;
   return FIM_OK;
 }
+
+// ---------------------------------------------------------------------------
+// allocation-free re-solve (no counterpart in the reference)
+//
+// Meant for callers that re-solve one staged mesh for many stimulus sets from
+// a loop sharing the device with other work: fim_set_stimuli replaces its
+// seed buffers (cudaFree, which waits for the whole device, then cudaMalloc,
+// which can fail once the caller's own pool holds the free memory).  Here the
+// stimuli and the solve's working set go to the fixed scratch of
+// fim_static.cu, the result to the caller's device buffer; the solver's own
+// buffers and last results are left as they were.
+extern "C" int fim_solve_noalloc(fim_solver *s, int64_t n, const int64_t *vertices, const double *t0,
+                                 double *d_phi, void *stream)
+{
+  if (!s) return set_err(nullptr, FIM_ERR_INVALID_ARGUMENT, "fim_solve_noalloc: solver is NULL");
+  if (!s->have_mesh || !s->have_cond)
+    return set_err(s, FIM_ERR_NOT_READY, "fim_solve_noalloc: mesh and conduction must be set first");
+  if (!d_phi) return set_err(s, FIM_ERR_INVALID_ARGUMENT, "fim_solve_noalloc: d_phi is NULL");
+  if (n < 0 || (n > 0 && (!vertices || !t0)))
+    return set_err(s, FIM_ERR_INVALID_ARGUMENT, "fim_solve_noalloc: bad count or NULL array");
+  if (s->nL > kStaticMaxCopies || s->nV > kStaticMaxVertices)
+    return set_err(s, FIM_ERR_INVALID_ARGUMENT,
+                   "fim_solve_noalloc: the mesh has %lld vertices (%lld vertex copies); the fixed scratch "
+                   "holds at most %lld of each -- use fim_set_stimuli + fim_solve",
+                   (long long)s->nV, (long long)s->nL, (long long)kStaticMaxCopies);
+  if (n > kStaticMaxSeeds)
+    return set_err(s, FIM_ERR_INVALID_ARGUMENT,
+                   "fim_solve_noalloc: %lld stimulus entries; the fixed scratch holds at most %lld",
+                   (long long)n, (long long)kStaticMaxSeeds);
+  int64_t entries = 0;  // stimulus entries once expanded to vertex copies
+  for (int64_t i = 0; i < n; ++i) {
+    const int64_t g = vertices[i];
+    if (g < 0 || g >= s->nV)
+      return set_err(s, FIM_ERR_INVALID_ARGUMENT, "fim_solve_noalloc: vertex %lld outside [0,%lld)",
+                     (long long)g, (long long)s->nV);
+    if (!std::isfinite(t0[i]))
+      return set_err(s, FIM_ERR_INVALID_ARGUMENT, "fim_solve_noalloc: start time %lld is not finite",
+                     (long long)i);
+    entries += s->h_gptr.empty() ? (s->in_tet[g] ? 1 : 0) : s->h_gptr[g + 1] - s->h_gptr[g];
+  }
+  if (entries > kStaticMaxSeedEntries)
+    return set_err(s, FIM_ERR_INVALID_ARGUMENT,
+                   "fim_solve_noalloc: the stimuli expand to %lld vertex copies; the fixed scratch holds at "
+                   "most %lld", (long long)entries, (long long)kStaticMaxSeedEntries);
+  CUDA_TRY(s, cudaSetDevice(s->device));
+  NoallocScratch sc{};
+  CUDA_TRY(s, noalloc_scratch(s->device, &sc));
+  cudaStream_t st = stream ? (cudaStream_t)stream : s->stream;
+  if (n > 0) {
+    CUDA_TRY(s, cudaMemcpyAsync(sc.raw_v, vertices, sizeof(int64_t) * n, cudaMemcpyHostToDevice, st));
+    CUDA_TRY(s, cudaMemcpyAsync(sc.raw_t, t0, sizeof(double) * n, cudaMemcpyHostToDevice, st));
+    CUDA_TRY(s, launch_noalloc_seeds(sc, (int32_t)n, s->gptr.p, s->gcopy.p, s->cptr.p, st));
+  }
+  const bool multi = s->gptr.p != nullptr;
+  FimDev d{};
+  d.nV = (int32_t)s->nL; d.nG = (int32_t)s->nV; d.nT = s->nT; d.nC = s->nC;
+  d.gptr = s->gptr.p; d.gcopy = s->gcopy.p;
+  d.phi_out = multi ? d_phi : nullptr; d.st_out = multi ? sc.st_out : nullptr;
+  d.cptr = s->cptr.p; d.cids = s->cids.p; d.cgeo = s->cgeo.p; d.cgf = s->cgf.p; d.nptr = s->nptr.p; d.nbr = s->nbr.p;
+  d.phi_f = sc.phi_f;
+  d.phi = sc.phi; d.phi2 = sc.phi2; d.st = sc.st; d.tst = sc.tst; d.flag = sc.flag;
+  d.list[0] = sc.list[0]; d.list[1] = sc.list[1]; d.list[2] = sc.list[2];
+  d.lfrozen = sc.lfrozen; d.lmarked = sc.lmarked; d.dec = sc.dec;
+  d.seed_v = sc.seed_v; d.seed_t = sc.seed_t; d.nseed = (int32_t)entries;
+  d.ctl = sc.ctl;
+  FimParams p{};
+  p.dt = s->opts.dt;
+  p.n_steps = s->opts.n_steps;
+  p.front_width = s->opts.front_width >= 0.0 ? s->opts.front_width : s->front_width;
+  p.apd = s->opts.apd;
+  p.max_iter = s->opts.max_iterations > 0 ? s->opts.max_iterations : 10000000;
+  p.timeout_ns = (uint64_t)(s->opts.timeout_s * 1e9);
+  p.withhold_block = 0;
+  p.exact_all = s->opts.exact_all ? 1 : 0;
+  CUDA_TRY(s, cudaMemsetAsync(sc.ctl, 0, sizeof(FimCtl), st));
+  CUDA_TRY(s, launch_solve(d, p, s->grid, s->block, st));
+  if (!multi) CUDA_TRY(s, launch_copy(sc.phi, d_phi, s->nV, st));
+  FimCtl ctl{};
+  CUDA_TRY(s, cudaMemcpyAsync(&ctl, sc.ctl, sizeof(FimCtl), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(s, cudaStreamSynchronize(st));
+  if (ctl.error == KERR_TIMEOUT)
+    return set_err(s, FIM_ERR_TIMEOUT, "fim_solve_noalloc: a grid barrier wait exceeded %.3f s (phase %d)",
+                   s->opts.timeout_s, ctl.error_where);
+  if (ctl.error == KERR_MAX_ITER)
+    return set_err(s, FIM_ERR_MAX_ITERATIONS, "fim_solve_noalloc: iteration cap %lld reached in a window",
+                   (long long)p.max_iter);
+  return FIM_OK;
+}

@@ -24,7 +24,7 @@ FAR, NEIG, NARROW, NEXT, FROZEN, TAIL = range(6)
 EXPORTS = ["fim_default_opts", "fim_create", "fim_destroy", "fim_last_error", "fim_set_mesh",
            "fim_set_conduction", "fim_set_conduction_device", "fim_set_stimuli", "fim_solve",
            "fim_get_times", "fim_get_times_device", "fim_get_stats", "fim_vtk_read", "fim_vtk_write",
-           "fim_read_tags", "fim_load_plan", "fim_set_stream"]
+           "fim_read_tags", "fim_load_plan", "fim_set_stream", "fim_solve_noalloc"]
 
 
 class FimOpts(C.Structure):
@@ -77,6 +77,7 @@ def lib():
         L.fim_get_times.argtypes = [vp, P(d), P(i32)]
         L.fim_get_times_device.argtypes = [vp, vp]
         L.fim_get_stats.argtypes = [vp, P(FimStats)]
+        L.fim_solve_noalloc.argtypes = [vp, i64, P(i64), P(d), vp, vp]
         L.fim_vtk_read.argtypes = [C.c_char_p, P(i64), P(i64), P(d), P(i64), P(i32)]
         L.fim_vtk_write.argtypes = [C.c_char_p, i64, i64, P(d), P(i64), P(i32), P(d), P(d)]
         L.fim_read_tags.argtypes = [C.c_char_p, P(i64), P(i32)]
@@ -172,6 +173,13 @@ class Solver:
 
     def times_device(self, dptr):
         _check(lib().fim_get_times_device(self.h, C.c_void_p(dptr)), self.h)
+
+    def solve_noalloc(self, vertices, t0, d_phi, stream=None):
+        """Allocation-free solve for these stimuli into device buffer d_phi (an address of n_vertices f64)."""
+        v = np.ascontiguousarray(vertices, dtype=np.int64)
+        t = np.ascontiguousarray(t0, dtype=np.float64)
+        _check(lib().fim_solve_noalloc(self.h, v.shape[0], _ptr(v, C.c_int64), _ptr(t, C.c_double),
+                                       C.c_void_p(d_phi), C.c_void_p(stream) if stream else None), self.h)
 
     def stats(self):
         s = FimStats()

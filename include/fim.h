@@ -129,6 +129,31 @@ typedef struct {
 } fim_stats;
 int fim_get_stats(const fim_solver *s, fim_stats *out);
 
+/* Allocation-free re-solve -- no counterpart in the reference.
+ * Solves s's mesh and conduction for the stimuli given here (host arrays,
+ * the rules of fim_set_stimuli) and writes the times of all n_vertices into
+ * d_phi (device memory on s's device), on `stream` (NULL = the solver's
+ * working stream), and waits for it.  Results are bit-identical to
+ * fim_set_stimuli + fim_solve + fim_get_times_device.
+ *
+ * It calls no allocator: the solve's working set lives in a fixed device
+ * array of the library (about 8 MB per device), for callers that must not
+ * allocate between solves -- e.g. a loop re-solving one mesh for many
+ * stimulus sets while other streams run, where fim_set_stimuli's
+ * cudaFree would wait for the whole device.  Limits: at most 131072 mesh
+ * vertices and 131072 vertex copies (one per submesh holding a vertex),
+ * 8192 stimulus entries, 32768 stimulus vertex copies; larger inputs are
+ * rejected with FIM_ERR_INVALID_ARGUMENT.  The solver's own buffers, stats
+ * and last results are not touched.
+ *
+ * The first call on a device resolves the array's address (and loads its
+ * code there); make it before any stream capture.  The array is shared by
+ * every call on that device in this process: calls that overlap in time
+ * (from several host threads) race on it and return wrong times, so they
+ * must be serialised by the caller. */
+int fim_solve_noalloc(fim_solver *s, int64_t n, const int64_t *vertices, const double *t0,
+                      double *d_phi, void *stream);
+
 /* Reference-compatible files.  fim_vtk_* read/write the legacy ASCII VTK
  * that the reference reads and writes (load_vtk / save_vtk,
  * src/io/vtk.cpp:11-211); fim_read_tags reads a partition file
