@@ -12,6 +12,9 @@ namespace fimgb {
 // Reference node states (types.h:85).
 enum : uint8_t { ST_FAR = 0, ST_NEIG = 1, ST_NARROW = 2, ST_NEXT = 3, ST_FROZEN = 4, ST_TAIL = 5 };
 
+// Threads per block of the persistent solve kernel (one block per SM).
+constexpr int kSolveThreads = 512;
+
 // Kernel error codes written into FimCtl::error.
 enum : int { KERR_NONE = 0, KERR_TIMEOUT = 1, KERR_MAX_ITER = 2 };
 

@@ -254,25 +254,6 @@ struct WarpCtx {
   int64_t nwarps;
 };
 
-// One FP64 local solve of the reference for corner c: kind 0..2 are the
-// triangle solves (1,2), (2,3), (1,3) and kind 3 the tet solve.  The caller
-// guarantees the neighbours the solve uses are valid.
-__device__ double exact_candidate(const FimDev &d, int64_t c, int kind)
-{
-  const int4 id = __ldg(d.cids + c);
-  const double p1 = __ldcg(d.phi + id.x), p2 = __ldcg(d.phi + id.y), p3 = __ldcg(d.phi + id.z);
-  const double2 *gp = reinterpret_cast<const double2 *>(d.cgeo + 10 * c);
-  double g[6];
-  {
-    const double2 t0 = __ldg(gp), t1 = __ldg(gp + 1), t2 = __ldg(gp + 2);
-    g[0] = t0.x; g[1] = t0.y; g[2] = t1.x; g[3] = t1.y; g[4] = t2.x; g[5] = t2.y;
-  }
-  if (kind == 3) return tet_ref(g[0], g[1], g[2], g[3], g[4], g[5], p1, p2, p3);
-  if (kind == 0) return tri_ref(g[3], g[4], g[5], p1, p2);
-  if (kind == 1) return tri_ref(g[1], g[5], g[2], p2, p3);
-  return tri_ref(g[0], g[4], g[2], p1, p3);
-}
-
 // Order-preserving map of doubles to unsigned integers, so that the minimum
 // of a vertex's candidates can be formed with integer atomicMin.
 __device__ __forceinline__ unsigned long long dkey(double x)
@@ -286,12 +267,17 @@ __device__ __forceinline__ double dunkey(unsigned long long k)
   return __longlong_as_double((long long)b);
 }
 
-constexpr int kThreads = 256;       // threads per block of the solve kernel
-constexpr int kSlots = 32;          // vertices per batch (at most)
-constexpr int kCornerCap = 768;     // corners per batch
-constexpr int kTriCap = 1024;       // triangle screens per batch (more are screened on the spot)
-constexpr int kTetCap = 768;        // tet screens per batch
-constexpr int kQcap = 512;          // exact solves queued per kind and batch
+// One block of 16 warps per SM: the FP64 solves of a batch are packed into
+// as few warps as possible, and those warps sit on different SM
+// sub-partitions (an FP64 warp instruction occupies its sub-partition's
+// FP64 pipe for 64 cycles whatever its active lanes, so two blocks per SM
+// would stack their FP64 warps on the same sub-partitions).
+constexpr int kThreads = kSolveThreads;  // threads per block of the solve kernel
+constexpr int kSlots = 64;          // vertices per batch (at most)
+constexpr int kCornerCap = 1536;    // corners per batch
+constexpr int kTriCap = 2048;       // triangle screens per batch (more are screened on the spot)
+constexpr int kTetCap = 1536;       // tet screens per batch
+constexpr int kQcap = 1024;         // exact solves queued per kind and batch
 
 // Order-preserving map of floats to unsigned integers (for atomicMin).
 __device__ __forceinline__ unsigned int fkey(float x)
@@ -304,43 +290,40 @@ __device__ __forceinline__ float funkey(unsigned int k)
   return __uint_as_float((k >> 31) ? (k & 0x7fffffffu) : ~k);
 }
 
-// Shared memory of one batch of vertex updates.
+// Shared memory of one batch of vertex updates.  Phase A loads everything a
+// corner's screens and decisions need once; the later phases read it from
+// here and go to global memory only for the FP64 operands of the solves
+// that survive the screens.
 struct BatchSh {
   int32_t vtx[kSlots];
+  int32_t cnt[kSlots];              // corners of each vertex
   int64_t c0[kSlots];
   int32_t cp[kSlots + 1];           // corner prefix over the batch's vertices
   double old[kSlots];
   unsigned long long res[kSlots];   // dkey of the running minimum (exact values)
   unsigned int bhi[kSlots];         // fkey of a float upper bound of the new time
-  // per corner of the batch: float times of the other three vertices,
-  // float edge lengths, validity bits
-  float pf[kCornerCap][3];
-  float sf[kCornerCap][3];
-  uint8_t vm[kCornerCap];
+  // per corner of the batch
+  int32_t nb[kCornerCap][3];        // the other three vertices
+  float pf[kCornerCap][3];          // their float times
+  float sf[kCornerCap][3];          // float edge lengths sqrt(e14), sqrt(e24), sqrt(e34)
+  float gf[kCornerCap][7];          // e13, e23, e34, e12, e14, e24 times 2^-k, and k
+  uint8_t vm[kCornerCap];           // validity bits of the three neighbours
+  uint8_t cs[kCornerCap];           // slot of the corner's vertex
   // compacted screen lists: item (corner j | pair k << 16) and lower bound
   uint32_t tri[kTriCap];
   float tri_lb[kTriCap];
   uint32_t tet[kTetCap];
   float tet_lb[kTetCap];
-  uint32_t q[2][kQcap];             // queued exact solves: [0] tets, [1] triangles
-  int ntri, ntet, nq[2];
+  uint32_t q[3][kQcap];             // queued exact solves: [0] tets, [1] triangles, [2] edges
+  int ntri, ntet, nq[3];
   int nslot;                        // vertices of the current batch
 };
 
-// Queue item: slot (5 bits) | kind (2 bits) | corner offset in the vertex (25 bits).
-__device__ __forceinline__ uint32_t make_item(int slot, int kind, int64_t off)
+// Queue item: slot (6 bits) | kind (2 bits) | corner index in the batch (24 bits).
+// kind: triangle pair 0..2 or 3 (tet) in queues 0 and 1, edge 0..2 in queue 2.
+__device__ __forceinline__ uint32_t make_item(int slot, int kind, int j)
 {
-  return (uint32_t)slot | ((uint32_t)kind << 5) | ((uint32_t)off << 7);
-}
-
-__device__ __forceinline__ int slot_of(const BatchSh &sh, int nslot, int j)
-{
-  int lo = 0, hi = nslot - 1;  // last slot with cp[slot] <= j
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (sh.cp[mid] <= j) lo = mid; else hi = mid - 1;
-  }
-  return lo;
+  return (uint32_t)slot | ((uint32_t)kind << 6) | ((uint32_t)j << 8);
 }
 
 // Appends one item per lane with `need` to a list in shared memory
@@ -355,45 +338,65 @@ __device__ __forceinline__ int warp_append(int *counter, bool need, int lane)
   return need ? base + __popc(mask & ((1u << lane) - 1u)) : -1;
 }
 
-// Queues an exact solve (or runs it on the spot when the queue is full).
-// qi (0: tets, 1: triangles) must be the same on every lane of the warp; the
-// item's kind may differ per lane.
-__device__ __forceinline__ void queue_exact(const FimDev &d, BatchSh &sh, bool need, int qi, int kind, int slot,
-                                            int64_t c, int lane)
+// One FP64 local solve of corner c with neighbours nb: kind 0..2 are the
+// triangle solves (1,2), (2,3), (1,3) and kind 3 the tet solve.
+__device__ __forceinline__ double exact_solve(const FimDev &d, int64_t c, int kind, const int32_t *nb)
+{
+  const double p1 = __ldcg(d.phi + nb[0]), p2 = __ldcg(d.phi + nb[1]), p3 = __ldcg(d.phi + nb[2]);
+  const double2 *gp = reinterpret_cast<const double2 *>(d.cgeo + 10 * c);
+  const double2 t0 = __ldg(gp), t1 = __ldg(gp + 1), t2 = __ldg(gp + 2);
+  if (kind == 3) return tet_ref(t0.x, t0.y, t1.x, t1.y, t2.x, t2.y, p1, p2, p3);
+  if (kind == 0) return tri_ref(t1.y, t2.x, t2.y, p1, p2);
+  if (kind == 1) return tri_ref(t0.y, t2.y, t1.x, p2, p3);
+  return tri_ref(t0.x, t2.x, t1.x, p1, p3);
+}
+
+// Edge candidate i (phi of neighbour i + its FP64 edge length) of corner c.
+__device__ __forceinline__ double exact_edge(const FimDev &d, int64_t c, int i, int32_t nbi)
+{
+  return __ldcg(d.phi + nbi) + __ldg(d.cgeo + 10 * c + 6 + i);
+}
+
+// Evaluates queued item `it` (queue qi) in FP64 and folds it into the minimum.
+__device__ __forceinline__ void run_item(const FimDev &d, BatchSh &sh, int qi, uint32_t it)
+{
+  const int slot = it & 63, kind = (it >> 6) & 3, j = (int)(it >> 8);
+  const int64_t c = sh.c0[slot] + (j - sh.cp[slot]);
+  const double val = qi == 2 ? exact_edge(d, c, kind, sh.nb[j][kind]) : exact_solve(d, c, kind, sh.nb[j]);
+  if (val < FIM_INF) atomicMin(&sh.res[slot], dkey(val));
+}
+
+// Queues an exact solve (or runs it on the spot when the queue is full).  qi
+// must be the same on every lane of the warp; the item's kind may differ.
+__device__ __forceinline__ void queue_exact(const FimDev &d, BatchSh &sh, bool need, int qi, int kind, int slot, int j,
+                                            int lane)
 {
   const int pos = warp_append(&sh.nq[qi], need, lane);
   if (pos < 0) return;
-  if (pos < kQcap) {
-    sh.q[qi][pos] = make_item(slot, kind, c - sh.c0[slot]);
-  } else {
-    const double val = exact_candidate(d, c, kind);
-    if (val < FIM_INF) atomicMin(&sh.res[slot], dkey(val));
-  }
+  const uint32_t it = make_item(slot, kind, j);
+  if (pos < kQcap) sh.q[qi][pos] = it;
+  else run_item(d, sh, qi, it);
 }
 
-// Triangle screen of pair k (0: (1,2), 1: (2,3), 2: (1,3)) of corner c.
-__device__ __forceinline__ CandBound tri_screen_of(const FimDev &d, int64_t c, int k, const float *pf)
+// FP32 screens of triangle pair k (0: (1,2), 1: (2,3), 2: (1,3)) and of the
+// tet of batch corner j, from the record in shared memory.
+__device__ __forceinline__ CandBound tri_screen_sm(const BatchSh &sh, int j, int k)
 {
-  const float4 *rp = reinterpret_cast<const float4 *>(d.cgf + 12 * c);
-  const float4 r0 = __ldg(rp), r1 = __ldg(rp + 1), r2 = __ldg(rp + 2);
-  const float tk = re_pow2f((int)r2.y);
-  // scaled e13, e23, e34, e12, e14, e24 -> true units
-  const float g[6] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y};
+  const float *g = sh.gf[j];
+  const float tk = re_pow2f((int)g[6]);
   const int i12 = k == 0 ? 3 : (k == 1 ? 1 : 0);   // e12 role
   const int i13 = k == 0 ? 4 : (k == 1 ? 5 : 4);   // e13 role
   const int i23 = k == 0 ? 5 : 2;                  // e23 role
   const int a = k == 0 ? 0 : (k == 1 ? 1 : 0), b = k == 0 ? 1 : 2;
   return tri_screen(re_scale(re_in(g[i12]), tk), re_scale(re_in(g[i13]), tk), re_scale(re_in(g[i23]), tk),
-                    re_in(pf[a]), re_in(pf[b]));
+                    re_in(sh.pf[j][a]), re_in(sh.pf[j][b]));
 }
 
-// Tet screen of corner c.
-__device__ __forceinline__ CandBound tet_screen_of(const FimDev &d, int64_t c, const float *pf)
+__device__ __forceinline__ CandBound tet_screen_sm(const BatchSh &sh, int j)
 {
-  const float4 *rp = reinterpret_cast<const float4 *>(d.cgf + 12 * c);
-  const float4 r0 = __ldg(rp), r1 = __ldg(rp + 1), r2 = __ldg(rp + 2);
-  const Re gs[6] = {re_in(r0.x), re_in(r0.y), re_in(r0.z), re_in(r0.w), re_in(r1.x), re_in(r1.y)};
-  return tet_screen(gs, re_in(pf[0]), re_in(pf[1]), re_in(pf[2]), (int)r2.y);
+  const float *g = sh.gf[j];
+  const Re gs[6] = {re_in(g[0]), re_in(g[1]), re_in(g[2]), re_in(g[3]), re_in(g[4]), re_in(g[5])};
+  return tet_screen(gs, re_in(sh.pf[j][0]), re_in(sh.pf[j][1]), re_in(sh.pf[j][2]), (int)g[6]);
 }
 
 // Writes a time and its float copy.
@@ -406,17 +409,18 @@ __device__ __forceinline__ void set_phi(const FimDev &d, int64_t v, double x)
 // One update phase over a vertex list.  Every block takes a contiguous part
 // of the list and processes it in batches of up to kSlots vertices / up to
 // kCornerCap corners, the corners of a batch spread over all threads:
-//  A -- load every corner: validity of the neighbours (state >= narrow and
-//       phi > phi_start - front_width, on the float copies when conclusive,
-//       else on the FP64 times), float edge bounds -> per-vertex upper bound
-//       bhi of the new time;
-//  B -- exact FP64 edge candidates that can still be the minimum; triangle
-//       and tet solves whose trivial bound min(neighbour times) <= bhi are
-//       appended to compacted screen lists (warp-ballot compaction);
+//  A -- load every corner once (neighbour ids, float screen record,
+//       neighbour states and float times), validity of the neighbours
+//       (state >= narrow and phi > phi_start - front_width, on the float
+//       copies when conclusive, else on the FP64 times), float edge bounds
+//       -> per-vertex upper bound bhi of the new time;
+//  B -- triangle and tet solves whose trivial bound min(neighbour times)
+//       <= bhi are appended to compacted screen lists (warp ballots);
 //  S -- the screens run over the lists with full warps (triangles and tets
 //       on separate warps); certain upper bounds tighten bhi;
-//  C -- solves whose lower bound does not exceed bhi are queued;
-//  D -- the queued solves run in FP64 (tets and triangles on separate warps);
+//  C -- solves and edges whose lower bound does not exceed bhi are queued;
+//  D -- the queued solves run in FP64 (tets, triangles and edges each from a
+//       warp boundary);
 //  E -- the reference's per-vertex decision on the exact minimum:
 //   mode 0 -- narrow vertices: window test (next), freeze test
 //             (cuda_fim.cu:2125-2163);
@@ -428,6 +432,7 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
                              float lower_lo, float lower_hi, double phi_start, double dt, bool exact_all, int s,
                              int64_t &n_filtered, int64_t &n_exact)
 {
+  constexpr int kPer = (kCornerCap + kThreads - 1) / kThreads;  // corners per thread in phase A
   const int tid = threadIdx.x, lane = tid & 31;
   const int64_t per_block = ((int64_t)n + gridDim.x - 1) / gridDim.x;
   const int64_t lbeg = min((int64_t)n, (int64_t)blockIdx.x * per_block);
@@ -441,93 +446,143 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
       const double old = __ldcg(d.phi + v);
       sh.vtx[tid] = v;
       sh.c0[tid] = d.cptr[v];
-      sh.cp[tid + 1] = (int32_t)(d.cptr[v + 1] - d.cptr[v]);
+      sh.cnt[tid] = (int32_t)(d.cptr[v + 1] - d.cptr[v]);
       sh.old[tid] = old;
       sh.res[tid] = dkey(old);
       sh.bhi[tid] = fkey(exact_all ? INFINITY : re_hi(re_in(__ldcg(d.phi_f + v))));
     }
     if (tid == 0) {
       sh.cp[0] = 0;
-      sh.ntri = 0; sh.ntet = 0; sh.nq[0] = 0; sh.nq[1] = 0;
+      sh.ntri = 0; sh.ntet = 0; sh.nq[0] = 0; sh.nq[1] = 0; sh.nq[2] = 0;
     }
     __syncthreads();
-    if (tid == 0) {
-      int k = 1;
-      for (; k <= cand; ++k) {
-        const int t = sh.cp[k - 1] + sh.cp[k];
-        if (t > kCornerCap && k > 1) break;
-        sh.cp[k] = t;
+    if (tid < 32) {
+      // inclusive prefix of the corner counts (slots lane and lane + 32)
+      int a = tid < cand ? sh.cnt[tid] : 0, b = tid + 32 < cand ? sh.cnt[tid + 32] : 0;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int ua = __shfl_up_sync(FULL_MASK, a, o), ub = __shfl_up_sync(FULL_MASK, b, o);
+        if (tid >= o) { a += ua; b += ub; }
       }
-      sh.nslot = k - 1;
+      b += __shfl_sync(FULL_MASK, a, 31);
+      sh.cp[tid + 1] = a;
+      sh.cp[tid + 33] = b;
+      // the longest run of slots with <= kCornerCap corners, at least one
+      const unsigned fa = __ballot_sync(FULL_MASK, tid < cand && a <= kCornerCap);
+      const unsigned fb = __ballot_sync(FULL_MASK, tid + 32 < cand && b <= kCornerCap);
+      if (tid == 0) sh.nslot = max(1, __popc(fa) + __popc(fb));
     }
     __syncthreads();
     const int nslot = sh.nslot;
     const int total = sh.cp[nslot];     // may exceed kCornerCap for a single huge vertex
     const int kept = min(total, kCornerCap);
 
-    // A: load, validity, float edge bounds
-    for (int j = tid; j < total; j += kThreads) {
-      const int slot = slot_of(sh, nslot, j);
+    // A: load, validity, float edge bounds.  Pass 1 copies every corner's
+    // neighbour ids and float screen record to shared memory, pass 2 loads
+    // the neighbours' states and float times; within a pass the loads of a
+    // thread's corners are independent, so they are all in flight together.
+    {
+      int slot[kPer];
+#pragma unroll
+      for (int r = 0; r < kPer; ++r) {
+        const int j = tid + r * kThreads;
+        slot[r] = 0;
+        if (j < kept) {
+          int lo = 0, hi = nslot - 1;  // last slot with cp[slot] <= j
+          while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (sh.cp[mid] <= j) lo = mid; else hi = mid - 1;
+          }
+          slot[r] = lo;
+          const int64_t c = sh.c0[lo] + (j - sh.cp[lo]);
+          const int4 id = __ldg(d.cids + c);
+          const float4 *rp = reinterpret_cast<const float4 *>(d.cgf + 12 * c);
+          const float4 r0 = __ldg(rp), r1 = __ldg(rp + 1), r2 = __ldg(rp + 2);
+          sh.nb[j][0] = id.x; sh.nb[j][1] = id.y; sh.nb[j][2] = id.z;
+          sh.sf[j][0] = r1.z; sh.sf[j][1] = r1.w; sh.sf[j][2] = r2.x;
+          sh.gf[j][0] = r0.x; sh.gf[j][1] = r0.y; sh.gf[j][2] = r0.z; sh.gf[j][3] = r0.w;
+          sh.gf[j][4] = r1.x; sh.gf[j][5] = r1.y; sh.gf[j][6] = r2.y;
+          sh.cs[j] = (uint8_t)lo;
+        }
+      }
+      float pf[kPer][3];
+      uint8_t stn[kPer][3];
+#pragma unroll
+      for (int r = 0; r < kPer; ++r) {
+        const int j = tid + r * kThreads;
+        if (j < kept) {
+#pragma unroll
+          for (int i = 0; i < 3; ++i) {
+            const int32_t nbi = sh.nb[j][i];
+            pf[r][i] = __ldcg(d.phi_f + nbi);
+            stn[r][i] = __ldcg(d.st + nbi);
+          }
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < kPer; ++r) {
+        const int j = tid + r * kThreads;
+        if (j >= kept) continue;
+        uint32_t m = 0;
+        float ub = INFINITY;
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+          const Re P = re_in(pf[r][i]);
+          bool ok = stn[r][i] >= ST_NARROW;
+          if (ok) {
+            if (re_lo(P) > lower_hi) ok = true;
+            else if (re_hi(P) <= lower_lo) ok = false;
+            else ok = __ldcg(d.phi + sh.nb[j][i]) > lower;
+          }
+          if (ok) {
+            m |= 1u << i;
+            ub = fminf(ub, re_hi(P + re_in(sh.sf[j][i])));
+          }
+          sh.pf[j][i] = pf[r][i];
+        }
+        if (m) ++n_filtered;
+        if (!exact_all && ub < INFINITY) atomicMin(&sh.bhi[slot[r]], fkey(ub));
+        sh.vm[j] = (uint8_t)m;
+      }
+    }
+    // corners beyond kCornerCap (a single vertex with very many corners):
+    // every solve of them goes to FP64
+    for (int j = kept + tid; j < total; j += kThreads) {
+      const int slot = 0;  // only a batch of one vertex has such corners
       const int64_t c = sh.c0[slot] + (j - sh.cp[slot]);
       const int4 id = __ldg(d.cids + c);
       const int32_t nb[3] = {id.x, id.y, id.z};
-      const float4 *rp = reinterpret_cast<const float4 *>(d.cgf + 12 * c);
-      const float4 r1 = __ldg(rp + 1), r2 = __ldg(rp + 2);
-      const float sv[3] = {r1.z, r1.w, r2.x};
       uint32_t m = 0;
-      float pf[3];
-      float ub = INFINITY;
-#pragma unroll
       for (int i = 0; i < 3; ++i) {
-        pf[i] = __ldcg(d.phi_f + nb[i]);
-        const Re P = re_in(pf[i]);
-        bool ok = __ldcg(d.st + nb[i]) >= ST_NARROW;
-        if (ok) {
-          if (re_lo(P) > lower_hi) ok = true;
-          else if (re_hi(P) <= lower_lo) ok = false;
-          else ok = __ldcg(d.phi + nb[i]) > lower;
-        }
-        if (ok) {
+        const double p = __ldcg(d.phi + nb[i]);
+        if (__ldcg(d.st + nb[i]) >= ST_NARROW && p > lower) {
           m |= 1u << i;
-          ub = fminf(ub, re_hi(P + re_in(sv[i])));
+          atomicMin(&sh.res[slot], dkey(p + __ldg(d.cgeo + 10 * c + 6 + i)));
         }
       }
       if (m) ++n_filtered;
-      if (!exact_all && ub < INFINITY) atomicMin(&sh.bhi[slot], fkey(ub));
-      if (j < kCornerCap) {
-        sh.vm[j] = (uint8_t)m;
-#pragma unroll
-        for (int i = 0; i < 3; ++i) { sh.pf[j][i] = pf[i]; sh.sf[j][i] = sv[i]; }
+      for (int k = 0; k < 4; ++k) {
+        const bool use = k == 3 ? m == 7u : (((m >> (k == 1 ? 1 : 0)) & 1u) && ((m >> (k == 0 ? 1 : 2)) & 1u));
+        if (!use) continue;
+        const double val = exact_solve(d, c, k, nb);
+        if (val < FIM_INF) atomicMin(&sh.res[slot], dkey(val));
       }
     }
     __syncthreads();
 
-    // B: exact edges; screen lists
+    // B: screen lists
     for (int jb = 0; jb < kept; jb += kThreads) {
       const int j = jb + tid;
       const bool in = j < kept;
       int slot = 0;
-      int64_t c = 0;
       uint32_t m = 0;
       float bhi = 0.f, lo[3] = {0.f, 0.f, 0.f};
       if (in) {
-        slot = slot_of(sh, nslot, j);
-        c = sh.c0[slot] + (j - sh.cp[slot]);
+        slot = sh.cs[j];
         m = sh.vm[j];
         bhi = funkey(sh.bhi[slot]);
-        const int4 id = __ldg(d.cids + c);
-        const int32_t nb[3] = {id.x, id.y, id.z};
 #pragma unroll
-        for (int i = 0; i < 3; ++i) {
-          const Re P = re_in(sh.pf[j][i]);
-          lo[i] = re_lo(P);
-          if ((m >> i) & 1u) {
-            if (!(re_lo(P + re_in(sh.sf[j][i])) > bhi)) {
-              const double val = __ldcg(d.phi + nb[i]) + __ldg(d.cgeo + 10 * c + 6 + i);
-              atomicMin(&sh.res[slot], dkey(val));
-            }
-          }
-        }
+        for (int i = 0; i < 3; ++i) lo[i] = re_lo(re_in(sh.pf[j][i]));
       }
       // triangle pairs (1,2), (2,3), (1,3) and the tet
 #pragma unroll
@@ -541,11 +596,8 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
           } else {  // list full: screen here
             CandBound cb;
             if (exact_all) { cb.some = CAND_SOME; cb.lb = NAN; cb.ub = INFINITY; }
-            else cb = tri_screen_of(d, c, k, sh.pf[j]);
-            if (cb.some && !(cb.lb > bhi)) {
-              const double val = exact_candidate(d, c, k);
-              if (val < FIM_INF) atomicMin(&sh.res[slot], dkey(val));
-            }
+            else cb = tri_screen_sm(sh, j, k);
+            if (cb.some && !(cb.lb > bhi)) run_item(d, sh, 1, make_item(slot, k, j));
           }
         }
       }
@@ -553,30 +605,6 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
         const bool need = in && m == 7u && !(fminf(lo[0], fminf(lo[1], lo[2])) > bhi);
         const int p = warp_append(&sh.ntet, need, lane);
         if (p >= 0) sh.tet[p] = (uint32_t)j;  // kTetCap == kCornerCap: never full
-      }
-    }
-    // corners beyond kCornerCap (a single vertex with very many corners):
-    // every solve of them goes to FP64
-    for (int jb = kept; jb < total; jb += kThreads) {
-      const int j = jb + tid;
-      if (j >= total) continue;
-      const int slot = slot_of(sh, nslot, j);
-      const int64_t c = sh.c0[slot] + (j - sh.cp[slot]);
-      const int4 id = __ldg(d.cids + c);
-      const int32_t nb[3] = {id.x, id.y, id.z};
-      uint32_t m = 0;
-      for (int i = 0; i < 3; ++i) {
-        const double p = __ldcg(d.phi + nb[i]);
-        if (__ldcg(d.st + nb[i]) >= ST_NARROW && p > lower) {
-          m |= 1u << i;
-          atomicMin(&sh.res[slot], dkey(p + __ldg(d.cgeo + 10 * c + 6 + i)));
-        }
-      }
-      for (int k = 0; k < 4; ++k) {
-        const bool use = k == 3 ? m == 7u : (((m >> (k == 1 ? 1 : 0)) & 1u) && ((m >> (k == 0 ? 1 : 2)) & 1u));
-        if (!use) continue;
-        const double val = exact_candidate(d, c, k);
-        if (val < FIM_INF) atomicMin(&sh.res[slot], dkey(val));
       }
     }
     __syncthreads();
@@ -589,66 +617,68 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
       for (int i = tid; i < tri0 + ntri; i += kThreads) {
         if (i < ntet) {
           const int j = (int)sh.tet[i];
-          const int slot = slot_of(sh, nslot, j);
-          const int64_t c = sh.c0[slot] + (j - sh.cp[slot]);
           CandBound cb;
           if (exact_all) { cb.some = CAND_SOME; cb.lb = NAN; cb.ub = INFINITY; }
-          else cb = tet_screen_of(d, c, sh.pf[j]);
+          else cb = tet_screen_sm(sh, j);
           sh.tet_lb[i] = !cb.some ? NAN : (isnan(cb.lb) ? -INFINITY : cb.lb);
-          if (!exact_all && cb.some && cb.ub < INFINITY) atomicMin(&sh.bhi[slot], fkey(cb.ub));
+          if (!exact_all && cb.some && cb.ub < INFINITY) atomicMin(&sh.bhi[sh.cs[j]], fkey(cb.ub));
         } else if (i >= tri0) {
           const int t = i - tri0;
           const int j = (int)(sh.tri[t] & 0xffffu), k = (int)(sh.tri[t] >> 16);
-          const int slot = slot_of(sh, nslot, j);
-          const int64_t c = sh.c0[slot] + (j - sh.cp[slot]);
           CandBound cb;
           if (exact_all) { cb.some = CAND_SOME; cb.lb = NAN; cb.ub = INFINITY; }
-          else cb = tri_screen_of(d, c, k, sh.pf[j]);
+          else cb = tri_screen_sm(sh, j, k);
           sh.tri_lb[t] = !cb.some ? NAN : (isnan(cb.lb) ? -INFINITY : cb.lb);
-          if (!exact_all && cb.some && cb.ub < INFINITY) atomicMin(&sh.bhi[slot], fkey(cb.ub));
+          if (!exact_all && cb.some && cb.ub < INFINITY) atomicMin(&sh.bhi[sh.cs[j]], fkey(cb.ub));
         }
       }
     }
     __syncthreads();
 
-    // C: queue the solves that can still be the minimum
+    // C: queue the solves and edges that can still be the minimum
     {
       const int ntet = min(sh.ntet, kTetCap), ntri = min(sh.ntri, kTriCap);
       for (int ib = 0; ib < ntet + ntri; ib += kThreads) {
         const int i = ib + tid;
         bool need = false;
-        int kind = 0, slot = 0;
-        int64_t c = 0;
+        int kind = 0, slot = 0, j = 0;
         if (i < ntet + ntri) {
-          int j;
           float l;
           if (i < ntet) { j = (int)sh.tet[i]; kind = 3; l = sh.tet_lb[i]; }
           else { const uint32_t it = sh.tri[i - ntet]; j = (int)(it & 0xffffu); kind = (int)(it >> 16); l = sh.tri_lb[i - ntet]; }
-          slot = slot_of(sh, nslot, j);
-          c = sh.c0[slot] + (j - sh.cp[slot]);
+          slot = sh.cs[j];
           need = l <= funkey(sh.bhi[slot]);  // NaN (no value) never
         }
         // separate ballots per queue keep each queue warp-compacted
-        queue_exact(d, sh, need && kind == 3, 0, kind, slot, c, lane);
-        queue_exact(d, sh, need && kind != 3, 1, kind, slot, c, lane);
+        queue_exact(d, sh, need && kind == 3, 0, kind, slot, j, lane);
+        queue_exact(d, sh, need && kind != 3, 1, kind, slot, j, lane);
+      }
+      for (int jb = 0; jb < kept; jb += kThreads) {
+        const int j = jb + tid;
+        const bool in = j < kept;
+        int slot = 0;
+        uint32_t m = 0;
+        float bhi = 0.f;
+        if (in) { slot = sh.cs[j]; m = sh.vm[j]; bhi = funkey(sh.bhi[slot]); }
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+          const bool need = in && ((m >> i) & 1u) && !(re_lo(re_in(sh.pf[j][i]) + re_in(sh.sf[j][i])) > bhi);
+          queue_exact(d, sh, need, 2, i, slot, j, lane);
+        }
       }
     }
     __syncthreads();
 
-    // D: exact solves; tets from thread 0, triangles from the next warp boundary
+    // D: exact solves; tets from thread 0, triangles and edges each from the
+    // next warp boundary
     {
-      const int ntet = min(sh.nq[0], kQcap), ntri = min(sh.nq[1], kQcap);
+      const int ntet = min(sh.nq[0], kQcap), ntri = min(sh.nq[1], kQcap), nedge = min(sh.nq[2], kQcap);
       const int tri0 = (ntet + 31) & ~31;
-      for (int j = tid; j < tri0 + ntri; j += kThreads) {
-        uint32_t it;
-        if (j < ntet) it = sh.q[0][j];
-        else if (j >= tri0) it = sh.q[1][j - tri0];
-        else continue;
-        const int slot = it & 31, kind = (it >> 5) & 3;
-        const int64_t c = sh.c0[slot] + (int64_t)(it >> 7);
-        const double val = exact_candidate(d, c, kind);
-        ++n_exact;
-        if (val < FIM_INF) atomicMin(&sh.res[slot], dkey(val));
+      const int edge0 = tri0 + ((ntri + 31) & ~31);
+      for (int j = tid; j < edge0 + nedge; j += kThreads) {
+        if (j < ntet) { run_item(d, sh, 0, sh.q[0][j]); ++n_exact; }
+        else if (j >= tri0 && j < tri0 + ntri) { run_item(d, sh, 1, sh.q[1][j - tri0]); ++n_exact; }
+        else if (j >= edge0) run_item(d, sh, 2, sh.q[2][j - edge0]);
       }
     }
     __syncthreads();
@@ -677,7 +707,7 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
   }
 }
 
-__global__ void __launch_bounds__(256) fim_solve_kernel(FimDev d, FimParams p)
+__global__ void __launch_bounds__(kThreads, 1) fim_solve_kernel(FimDev d, FimParams p)
 {
   FimCtl *ctl = d.ctl;
   const uint32_t nblocks = gridDim.x;
@@ -689,7 +719,8 @@ __global__ void __launch_bounds__(256) fim_solve_kernel(FimDev d, FimParams p)
   w.nwarps = nthreads >> 5;
   int64_t my_evals = 0, my_updates = 0, my_exact = 0;
   int where = 0;
-  __shared__ BatchSh sh;
+  extern __shared__ __align__(16) unsigned char fim_smem[];
+  BatchSh &sh = *reinterpret_cast<BatchSh *>(fim_smem);
 
   // reset_states_gpu + update_events_gpu: phi = INF, far; seeds narrow.
   for (int64_t v = gtid; v < d.nV; v += nthreads) {
@@ -879,7 +910,9 @@ cudaError_t solve_grid_size(int device, int block, int *grid)
   int sms = 0, per_sm = 0;
   cudaError_t e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
   if (e != cudaSuccess) return e;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fim_solve_kernel, block, 0);
+  e = cudaFuncSetAttribute(fim_solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(BatchSh));
+  if (e != cudaSuccess) return e;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fim_solve_kernel, block, sizeof(BatchSh));
   if (e != cudaSuccess) return e;
   if (per_sm < 1) per_sm = 1;
   *grid = sms * per_sm;
@@ -891,7 +924,8 @@ cudaError_t launch_solve(const FimDev &d, const FimParams &p, int grid, int bloc
   FimDev dd = d;
   FimParams pp = p;
   void *args[] = {&dd, &pp};
-  return cudaLaunchCooperativeKernel((const void *)fim_solve_kernel, dim3(grid), dim3(block), args, 0, stream);
+  return cudaLaunchCooperativeKernel((const void *)fim_solve_kernel, dim3(grid), dim3(block), args, sizeof(BatchSh),
+                                     stream);
 }
 
 __global__ void fim_copy_kernel(const double *__restrict__ src, double *__restrict__ dst, int64_t n)

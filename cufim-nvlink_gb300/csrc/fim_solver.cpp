@@ -68,7 +68,7 @@ struct fim_solver {
   cudaStream_t stream = nullptr;      // working stream (own_stream unless fim_set_stream)
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   std::string err;
-  int grid = 0, block = 256;
+  int grid = 0, block = kSolveThreads;
 
   // mesh (nL vertex copies: nL == nV with one submesh)
   int64_t nV = 0, nT = 0, nC = 0, nL = 0;

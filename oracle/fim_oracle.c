@@ -9,7 +9,7 @@
  * Pinning: the local solver, the metric/edge-norm precompute and the
  * per-aggregate vertex numbering are compared bit-for-bit against the
  * reference's own code compiled on the host (oracle/_ref, built from the
- * reference sources by oracle/build_ref.py).  The FIM state machine is pinned
+ * reference sources by oracle/build.py).  The FIM state machine is pinned
  * by analytic known answers and by the reference's golden output on its unit
  * mesh (tests/golden).
  *

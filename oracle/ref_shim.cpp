@@ -1,6 +1,6 @@
 // ref_shim.cpp -- extern "C" entry points over the reference's own code,
 // compiled for the host from the reference sources where they lie
-// (oracle/build_ref.py).  TEST INFRASTRUCTURE ONLY: it lets the tests compare
+// (oracle/build.py).  TEST INFRASTRUCTURE ONLY: it lets the tests compare
 // the C restatement in fim_oracle.c, and the product's I/O, with the
 // reference's code on the same inputs.  Nothing here is product code.
 //
