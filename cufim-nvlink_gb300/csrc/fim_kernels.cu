@@ -275,7 +275,7 @@ __device__ __forceinline__ double dunkey(unsigned long long k)
 constexpr int kThreads = kSolveThreads;  // threads per block of the solve kernel
 constexpr int kSlots = 64;          // vertices per batch (at most)
 constexpr int kCornerCap = 1536;    // corners per batch
-constexpr int kTriCap = 2048;       // triangle screens per batch (more are screened on the spot)
+constexpr int kTriCap = 3 * kCornerCap;  // triangle screens per batch: never full
 constexpr int kTetCap = 1536;       // tet screens per batch
 constexpr int kQcap = 1024;         // exact solves queued per kind and batch
 
