@@ -36,6 +36,10 @@ for _p in (ROOT, PKG):
 import numpy as np  # noqa: E402
 
 SLAB_CELLS = (266, 93, 40)
+# DRAM bytes (read + write) of one fim_solve_kernel launch per vertex update,
+# from ncu dram__bytes_read.sum + dram__bytes_write.sum on this workload
+# (6.110 GB for 4,689,493 vertex updates; profiles/fim_solve_kernel_slab266x93x40_launches.md)
+NCU_DRAM_BYTES_PER_VERTEX_UPDATE = 6.110e9 / 4689493
 METRIC = "slab solves/s (1.03M-vertex anisotropic FIM, bit-exact vs FP64 oracle)"
 UNIT = "solves/s"
 
@@ -268,6 +272,7 @@ def run_mine(args):
         s.close()
         return
     b_vu = 40.0 * nT / nV + 9.0
+    cells_default = args.cells is None
     upd = stats["vertex_updates"]
     mean_solve_ms = float(np.mean(solve_ms))
     achieved = upd * b_vu / (mean_solve_ms * 1e-3) / 1e9
@@ -281,10 +286,13 @@ def run_mine(args):
         "vertex_updates_per_s": upd / (mean_solve_ms * 1e-3), "corners_screened": stats["corner_evals"],
         "fp64_local_solves": stats["exact_evals"],
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": achieved / hbm_peak, "traffic": None,
+                     "frac": achieved / hbm_peak,
+                     "traffic": NCU_DRAM_BYTES_PER_VERTEX_UPDATE * upd if cells_default else None,
                      "kernel": "fim_solve_kernel", "bytes_per_vertex_update": b_vu,
                      "peak_source": peak_src,
-                     "note": "FP64-pipe bound on GB300; algorithmic bytes per SURVEY model"},
+                     "traffic_source": "ncu DRAM bytes per vertex update of the same workload x this run's updates",
+                     "note": ("algorithmic bytes = vertex updates x (40 T/V + 9) B; the kernel is bound by the "
+                              "latency of its per-batch phase chain (FP64 solves, block barriers), not by HBM")},
         "e2e": {"value": world * e2e_steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": 2 * args.steps,
