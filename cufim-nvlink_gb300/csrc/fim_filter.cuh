@@ -205,4 +205,110 @@ __device__ __forceinline__ CandBound tet_screen(const Re *g, Re p1, Re p2, Re p3
   return r;
 }
 
+// Per-corner lower bounds, in true units, of the square-root term of the
+// reference's local solves, from the scaled squared edge norms
+// g = e13, e23, e34, e12, e14, e24 (times 2^-k, k even):
+//  * triangle pair (1,2), (2,3), (1,3): solve_tri_cu's root term is the
+//    metric distance from the target "4" to the point l x_a + (1-l) x_b of
+//    the pair's segment (its a + 2 l b + l^2 c is that squared distance), so
+//    the distance from "4" to the segment bounds it: foot
+//    lambda* = (Sb - (Sa + Sb - B)/2) / B; inside (0,1) the line distance
+//    h^2 = (Sa Sb - ((Sa + Sb - B)/2)^2) / B, else min(Sa, Sb);
+//  * tet: solve_tet_cu's root term is sqrt(Q(l1, l2)) with the reference's
+//    Q = a + 2 l1 b + l1^2 c + 2 l1 l2 d + 2 l2 e + l2^2 f (cuda_fim.h:1302-1360;
+//    not a distance), at an accepted root (l1, l2, 1 - l1 - l2 > 0), so the
+//    minimum of Q over the closed triangle l1, l2 >= 0, l1 + l2 <= 1 bounds
+//    it: the minimum over the three edges (1D quadratics) and, when the
+//    Hessian is certainly positive definite, the unconstrained minimum.
+// A solve's value is a convex combination of its times plus that term, so
+// min(times) + bound is below every value it returns (up to roundings the
+// caller adds).  Undecidable or degenerate cases give 0 (no bound).
+__device__ __forceinline__ float root_lo(Re q, float emax, float tk)
+{
+  // the solves' own rounding of the squared term is absolute and below
+  // 2^-23 emax (the triangle solve squares its float l: 2^-24 e12; FP64
+  // roundings: below 2^-45 emax); then the rounding of the square root
+  const float lo = re_lo(q) - 0x1p-22f * emax;
+  if (!(lo > 0.f)) return 0.f;
+  const float h = sqrtf(lo) * (1.f - 0x1p-22f);
+  const float r = h * tk;
+  return isfinite(r) ? r : 0.f;
+}
+
+__device__ __forceinline__ float segment_lo(Re B, Re Sa, Re Sb, float emax, float tk)
+{
+  const Re uw = re_scale((Sa + Sb) - B, 0.5f);
+  const Re lam = re_div(Sb - uw, B);
+  if (re_hi(lam) <= 0.f) return root_lo(Sb, emax, tk);
+  if (re_lo(lam) >= 1.f) return root_lo(Sa, emax, tk);
+  return root_lo(re_div(Sa * Sb - uw * uw, B), emax, tk);  // line distance <= segment distance
+}
+
+// re_lo, with NaN (an overflowed bound) turned into -inf, so that a minimum
+// over candidates never drops it
+__device__ __forceinline__ float safe_lo(Re a)
+{
+  const float l = re_lo(a);
+  return l == l ? l : -INFINITY;
+}
+
+// Lower bound of the minimum over s in [0,1] of al + 2 be s + ga s^2.
+__device__ __forceinline__ float quad01_lo(Re al, Re be, Re ga)
+{
+  const float ends = fminf(safe_lo(al), safe_lo((al + re_scale(be, 2.f)) + ga));
+  if (re_hi(ga) <= 0.f) return ends;         // concave or linear: the minimum is at an end
+  if (!(re_lo(ga) > 0.f)) return -INFINITY;  // curvature sign undecided: no bound
+  const Re s = re_div(-be, ga);              // vertex of the parabola
+  if (re_hi(s) <= 0.f || re_lo(s) >= 1.f) return ends;
+  return fminf(ends, safe_lo(al - re_div(be * be, ga)));
+}
+
+__device__ __forceinline__ void corner_bounds(const float *gs, int k, float *h)
+{
+  const Re e13 = re_in(gs[0]), e23 = re_in(gs[1]), e34 = re_in(gs[2]);
+  const Re e12 = re_in(gs[3]), e14 = re_in(gs[4]), e24 = re_in(gs[5]);
+  float emax = 0.f;
+  bool finite = true;
+#pragma unroll
+  for (int i = 0; i < 6; ++i) { emax = fmaxf(emax, gs[i]); finite = finite && isfinite(gs[i]); }
+  const float tk = re_pow2f(k / 2);
+  h[0] = h[1] = h[2] = h[3] = 0.f;
+  if (!finite || !(emax > 0.f) || !isfinite(tk)) return;
+  h[0] = segment_lo(e12, e14, e24, emax, tk);   // pair (1,2)
+  h[1] = segment_lo(e23, e24, e34, emax, tk);   // pair (2,3)
+  h[2] = segment_lo(e13, e14, e34, emax, tk);   // pair (1,3)
+  // the tet's Q with the reference's coefficients
+  const Re A = e13;
+  const Re B = re_scale((e23 + e13) - e12, 0.5f);
+  const Re C = re_scale((e34 + e13) - e14, -0.5f);
+  const Re D = e23;
+  const Re E = re_scale((e34 + e23) - e24, -0.5f);
+  const Re F = e34;
+  float qmin = quad01_lo(A, B, C);                                   // l2 = 0
+  qmin = fminf(qmin, quad01_lo(A, E, F));                            // l1 = 0
+  qmin = fminf(qmin, quad01_lo((A + re_scale(B, 2.f)) + C,           // l1 = 1 - s, l2 = s
+                               ((D + E) - B) - C, (C - re_scale(D, 2.f)) + F));
+  // an interior minimum needs a positive definite Hessian (c > 0, cf - d^2 > 0);
+  // unless that is excluded, the unconstrained minimum
+  // a - (f b^2 - 2 d b e + c e^2) / (cf - d^2) joins the candidates (-inf when
+  // the determinant's sign is undecided)
+  const Re det = C * F - D * D;
+  if (!(re_hi(C) <= 0.f || re_hi(det) <= 0.f)) {
+    const Re num = ((F * B) * B - re_scale((D * B) * E, 2.f)) + (C * E) * E;
+    qmin = fminf(qmin, safe_lo(A - re_div(num, det)));
+  }
+  h[3] = root_lo(re_make(qmin, 0.f), emax, tk);
+}
+
+// Lower bound of every value a triangle or tet solve can return, given the
+// float lower bound m_lo of the minimum and an upper bound m_hi of the
+// maximum of its times and the distance bound h: covers the float rounding
+// of the sum and of the reference's float-typed triangle result and the FP64
+// roundings of both solves.
+__device__ __forceinline__ float solve_lo(float m_lo, float m_hi, float h)
+{
+  const float x = m_lo + h;
+  return x - 0x1p-21f * (fabsf(m_lo) + fabsf(m_hi) + h);
+}
+
 }  // namespace fimgb

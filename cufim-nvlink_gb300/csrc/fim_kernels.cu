@@ -170,10 +170,16 @@ __global__ void fim_metric_kernel(const int32_t *__restrict__ tslots, const int6
       o[3] = g[sel_of(t, 3)]; o[4] = g[sel_of(t, 4)]; o[5] = g[sel_of(t, 5)];
       o[6] = s[sel_of(t, 4)]; o[7] = s[sel_of(t, 5)]; o[8] = s[sel_of(t, 2)];
       o[9] = 0.0;
-      float4 *of = reinterpret_cast<float4 *>(cgf + 12 * c);
-      of[0] = make_float4((float)(o[0] * sg), (float)(o[1] * sg), (float)(o[2] * sg), (float)(o[3] * sg));
-      of[1] = make_float4((float)(o[4] * sg), (float)(o[5] * sg), (float)o[6], (float)o[7]);
+      float4 *of = reinterpret_cast<float4 *>(cgf + kCgfStride * c);
+      const float gs[6] = {(float)(o[0] * sg), (float)(o[1] * sg), (float)(o[2] * sg),
+                           (float)(o[3] * sg), (float)(o[4] * sg), (float)(o[5] * sg)};
+      float hb[4];
+      corner_bounds(gs, ok ? ks : 0, hb);
+      if (!ok) hb[0] = hb[1] = hb[2] = hb[3] = 0.f;
+      of[0] = make_float4(gs[0], gs[1], gs[2], gs[3]);
+      of[1] = make_float4(gs[4], gs[5], (float)o[6], (float)o[7]);
       of[2] = make_float4((float)o[8], (float)ks, ok ? 0.f : 1.f, 0.f);
+      of[3] = make_float4(hb[0], hb[1], hb[2], hb[3]);
     }
   }
 }
@@ -307,6 +313,7 @@ struct BatchSh {
   float pf[kCornerCap][3];          // their float times
   float sf[kCornerCap][3];          // float edge lengths sqrt(e14), sqrt(e24), sqrt(e34)
   float gf[kCornerCap][7];          // e13, e23, e34, e12, e14, e24 times 2^-k, and k
+  float lbt[kCornerCap][4];         // root-term bounds, then lower bounds of pairs (1,2), (2,3), (1,3) and tet
   uint8_t vm[kCornerCap];           // validity bits of the three neighbours
   uint8_t cs[kCornerCap];           // slot of the corner's vertex
   // compacted screen lists: item (corner j | pair k << 16) and lower bound
@@ -496,8 +503,9 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
           slot[r] = lo;
           const int64_t c = sh.c0[lo] + (j - sh.cp[lo]);
           const int4 id = __ldg(d.cids + c);
-          const float4 *rp = reinterpret_cast<const float4 *>(d.cgf + 12 * c);
-          const float4 r0 = __ldg(rp), r1 = __ldg(rp + 1), r2 = __ldg(rp + 2);
+          const float4 *rp = reinterpret_cast<const float4 *>(d.cgf + kCgfStride * c);
+          const float4 r0 = __ldg(rp), r1 = __ldg(rp + 1), r2 = __ldg(rp + 2), r3 = __ldg(rp + 3);
+          sh.lbt[j][0] = r3.x; sh.lbt[j][1] = r3.y; sh.lbt[j][2] = r3.z; sh.lbt[j][3] = r3.w;
           sh.nb[j][0] = id.x; sh.nb[j][1] = id.y; sh.nb[j][2] = id.z;
           sh.sf[j][0] = r1.z; sh.sf[j][1] = r1.w; sh.sf[j][2] = r2.x;
           sh.gf[j][0] = r0.x; sh.gf[j][1] = r0.y; sh.gf[j][2] = r0.z; sh.gf[j][3] = r0.w;
@@ -543,6 +551,18 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
         if (m) ++n_filtered;
         if (!exact_all && ub < INFINITY) atomicMin(&sh.bhi[slot[r]], fkey(ub));
         sh.vm[j] = (uint8_t)m;
+        // lower bounds of the triangle pairs and the tet: min(times) + root-term bound
+        float lo[3], hi[3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+          const Re P = re_in(pf[r][i]);
+          lo[i] = re_lo(P);
+          hi[i] = re_hi(P);
+        }
+        sh.lbt[j][0] = solve_lo(fminf(lo[0], lo[1]), fmaxf(hi[0], hi[1]), sh.lbt[j][0]);
+        sh.lbt[j][1] = solve_lo(fminf(lo[1], lo[2]), fmaxf(hi[1], hi[2]), sh.lbt[j][1]);
+        sh.lbt[j][2] = solve_lo(fminf(lo[0], lo[2]), fmaxf(hi[0], hi[2]), sh.lbt[j][2]);
+        sh.lbt[j][3] = solve_lo(fminf(lo[0], fminf(lo[1], lo[2])), fmaxf(hi[0], fmaxf(hi[1], hi[2])), sh.lbt[j][3]);
       }
     }
     // corners beyond kCornerCap (a single vertex with very many corners):
@@ -576,19 +596,19 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
       const bool in = j < kept;
       int slot = 0;
       uint32_t m = 0;
-      float bhi = 0.f, lo[3] = {0.f, 0.f, 0.f};
+      float bhi = 0.f, lb[4] = {0.f, 0.f, 0.f, 0.f};
       if (in) {
         slot = sh.cs[j];
         m = sh.vm[j];
         bhi = funkey(sh.bhi[slot]);
 #pragma unroll
-        for (int i = 0; i < 3; ++i) lo[i] = re_lo(re_in(sh.pf[j][i]));
+        for (int i = 0; i < 4; ++i) lb[i] = sh.lbt[j][i];
       }
       // triangle pairs (1,2), (2,3), (1,3) and the tet
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
         const int a = k == 1 ? 1 : 0, b = k == 0 ? 1 : 2;
-        const bool need = in && ((m >> a) & 1u) && ((m >> b) & 1u) && !(fminf(lo[a], lo[b]) > bhi);
+        const bool need = in && ((m >> a) & 1u) && ((m >> b) & 1u) && !(lb[k] > bhi);
         const int p = warp_append(&sh.ntri, need, lane);
         if (p >= 0) {
           if (p < kTriCap) {
@@ -602,7 +622,7 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
         }
       }
       {
-        const bool need = in && m == 7u && !(fminf(lo[0], fminf(lo[1], lo[2])) > bhi);
+        const bool need = in && m == 7u && !(lb[3] > bhi);
         const int p = warp_append(&sh.ntet, need, lane);
         if (p >= 0) sh.tet[p] = (uint32_t)j;  // kTetCap == kCornerCap: never full
       }

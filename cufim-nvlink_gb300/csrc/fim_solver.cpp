@@ -404,7 +404,7 @@ extern "C" int fim_set_mesh(fim_solver *s, int64_t nV, const double *xyz, int64_
   CUDA_TRY(s, s->cptr.alloc(nL + 1));
   CUDA_TRY(s, s->cids.alloc(nC));
   CUDA_TRY(s, s->cgeo.alloc(10 * nC));
-  CUDA_TRY(s, s->cgf.alloc(12 * nC));
+  CUDA_TRY(s, s->cgf.alloc((size_t)kCgfStride * nC));
   CUDA_TRY(s, s->nptr.alloc(nL + 1));
   CUDA_TRY(s, s->nbr.alloc(nbr.size()));
   CUDA_TRY(s, s->fib.alloc(3 * nT));
