@@ -39,6 +39,10 @@ struct Re {
 __device__ __forceinline__ Re re_make(float v, float e) { Re r; r.v = v; r.e = e; return r; }
 // float copy of an FP64 operand (round to nearest)
 __device__ __forceinline__ Re re_in(float v) { return re_make(v, fmaf(fabsf(v), 0x1p-24f, FIM_RE_TINY)); }
+// float edge length (sqrtf of the scaled float norm times 2^(k/2)): within
+// 1.5 * 2^-24 relative of the FP64 sqrt of the FP64 norm, plus an absolute
+// 2^-48 for norms that the scaling pushes into the subnormal range
+__device__ __forceinline__ Re re_len(float v) { return re_make(v, fmaf(fabsf(v), 0x1p-23f, 0x1p-48f)); }
 __device__ __forceinline__ Re operator+(Re a, Re b)
 {
   const float v = a.v + b.v;

@@ -12,6 +12,8 @@ namespace fimgb {
 // Reference node states (types.h:85).
 enum : uint8_t { ST_FAR = 0, ST_NEIG = 1, ST_NARROW = 2, ST_NEXT = 3, ST_FROZEN = 4, ST_TAIL = 5 };
 
+// Doubles per corner of the FP64 record.
+constexpr int kCgeoStride = 6;
 // Floats per corner of the FP32 screen record.
 constexpr int kCgfStride = 16;
 
@@ -57,7 +59,7 @@ struct FimDev {
   // topology
   const int64_t *cptr;        // [nV+1] corner range per vertex
   const int4 *cids;           // [nC] other three vertices of the corner ("1","2","3"), w unused
-  const double *cgeo;         // [nC*10] e13,e23,e34,e12,e14,e24, sqrt(e14), sqrt(e24), sqrt(e34), pad
+  const double *cgeo;         // [nC*kCgeoStride] FP64 e13, e23, e34, e12, e14, e24
   const float *cgf;           // [nC*kCgfStride] float screen record: e13..e24 * 2^-k, sqrt(e14,e24,e34), k, bad,
                               //   pad, root-term bounds of pairs (1,2), (2,3), (1,3) and of the tet
   float *phi_f;               // float copy (round to nearest) of phi, kept in step with it

@@ -142,7 +142,7 @@ __global__ void fim_metric_kernel(const int32_t *__restrict__ tslots, const int6
     const int32_t v2 = tslots[4 * e + 2], v3 = tslots[4 * e + 3];
     const int32_t va[6] = {v0, v0, v1, v0, v1, v2};
     const int32_t vb[6] = {v1, v2, v2, v3, v3, v3};
-    double g[6], s[6];
+    double g[6];
 #pragma unroll
     for (int k = 0; k < 6; ++k) {
       // load_edge(a, b) = x_a - x_b (types.h:210-216); aMb_sym (types.h:165-171)
@@ -150,7 +150,6 @@ __global__ void fim_metric_kernel(const int32_t *__restrict__ tslots, const int6
       const double ey = xyz[3 * (int64_t)va[k] + 1] - xyz[3 * (int64_t)vb[k] + 1];
       const double ez = xyz[3 * (int64_t)va[k] + 2] - xyz[3 * (int64_t)vb[k] + 2];
       g[k] = (M0*ex + M1*ey + M2*ez)*ex + (M1*ex + M3*ey + M4*ez)*ey + (M2*ex + M4*ey + M5*ez)*ez;
-      s[k] = sqrt(g[k]);
     }
     // scale 2^-k (k even) of the float screen record: edge norms O(1)
     double gmax = g[0];
@@ -162,23 +161,33 @@ __global__ void fim_metric_kernel(const int32_t *__restrict__ tslots, const int6
     const bool ok = isfinite(gmax) && gmax > 0.0 && ks <= 50 && ks >= -50;
     if (!ok) ks = 0;
     const double sg = ldexp(1.0, -ks);
+    const float tk = ldexpf(1.f, ks / 2);
+    // FP32 copies of the edge norms (scaled) and of the three edge lengths
+    // towards each corner: sqrtf of the scaled norm times 2^(k/2), within
+    // 1.5 * 2^-24 of the FP64 sqrt the reference adds (the FP64 lengths
+    // themselves are taken where an edge candidate is evaluated exactly)
+    float gsc[6], len[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+      gsc[k] = (float)(g[k] * sg);
+      len[k] = sqrtf(gsc[k]) * tk;
+    }
 #pragma unroll
     for (int t = 0; t < 4; ++t) {
       const int64_t c = cidx[4 * e + t];
-      double *o = cgeo + 10 * c;
-      o[0] = g[sel_of(t, 0)]; o[1] = g[sel_of(t, 1)]; o[2] = g[sel_of(t, 2)];
-      o[3] = g[sel_of(t, 3)]; o[4] = g[sel_of(t, 4)]; o[5] = g[sel_of(t, 5)];
-      o[6] = s[sel_of(t, 4)]; o[7] = s[sel_of(t, 5)]; o[8] = s[sel_of(t, 2)];
-      o[9] = 0.0;
+      double2 *o = reinterpret_cast<double2 *>(cgeo + kCgeoStride * c);
+      o[0] = make_double2(g[sel_of(t, 0)], g[sel_of(t, 1)]);
+      o[1] = make_double2(g[sel_of(t, 2)], g[sel_of(t, 3)]);
+      o[2] = make_double2(g[sel_of(t, 4)], g[sel_of(t, 5)]);
       float4 *of = reinterpret_cast<float4 *>(cgf + kCgfStride * c);
-      const float gs[6] = {(float)(o[0] * sg), (float)(o[1] * sg), (float)(o[2] * sg),
-                           (float)(o[3] * sg), (float)(o[4] * sg), (float)(o[5] * sg)};
+      const float gs[6] = {gsc[sel_of(t, 0)], gsc[sel_of(t, 1)], gsc[sel_of(t, 2)],
+                           gsc[sel_of(t, 3)], gsc[sel_of(t, 4)], gsc[sel_of(t, 5)]};
       float hb[4];
       corner_bounds(gs, ok ? ks : 0, hb);
       if (!ok) hb[0] = hb[1] = hb[2] = hb[3] = 0.f;
       of[0] = make_float4(gs[0], gs[1], gs[2], gs[3]);
-      of[1] = make_float4(gs[4], gs[5], (float)o[6], (float)o[7]);
-      of[2] = make_float4((float)o[8], (float)ks, ok ? 0.f : 1.f, 0.f);
+      of[1] = make_float4(gs[4], gs[5], len[sel_of(t, 4)], len[sel_of(t, 5)]);
+      of[2] = make_float4(len[sel_of(t, 2)], (float)ks, ok ? 0.f : 1.f, 0.f);
       of[3] = make_float4(hb[0], hb[1], hb[2], hb[3]);
     }
   }
@@ -350,7 +359,7 @@ __device__ __forceinline__ int warp_append(int *counter, bool need, int lane)
 __device__ __forceinline__ double exact_solve(const FimDev &d, int64_t c, int kind, const int32_t *nb)
 {
   const double p1 = __ldcg(d.phi + nb[0]), p2 = __ldcg(d.phi + nb[1]), p3 = __ldcg(d.phi + nb[2]);
-  const double2 *gp = reinterpret_cast<const double2 *>(d.cgeo + 10 * c);
+  const double2 *gp = reinterpret_cast<const double2 *>(d.cgeo + kCgeoStride * c);
   const double2 t0 = __ldg(gp), t1 = __ldg(gp + 1), t2 = __ldg(gp + 2);
   if (kind == 3) return tet_ref(t0.x, t0.y, t1.x, t1.y, t2.x, t2.y, p1, p2, p3);
   if (kind == 0) return tri_ref(t1.y, t2.x, t2.y, p1, p2);
@@ -358,10 +367,14 @@ __device__ __forceinline__ double exact_solve(const FimDev &d, int64_t c, int ki
   return tri_ref(t0.x, t2.x, t1.x, p1, p3);
 }
 
+// Position of e14, e24, e34 (the edges from neighbour 0, 1, 2 to the corner's
+// vertex) in a corner record.
+__device__ __forceinline__ int edge_slot(int i) { return i == 0 ? 4 : (i == 1 ? 5 : 2); }
+
 // Edge candidate i (phi of neighbour i + its FP64 edge length) of corner c.
 __device__ __forceinline__ double exact_edge(const FimDev &d, int64_t c, int i, int32_t nbi)
 {
-  return __ldcg(d.phi + nbi) + __ldg(d.cgeo + 10 * c + 6 + i);
+  return __ldcg(d.phi + nbi) + sqrt(__ldg(d.cgeo + kCgeoStride * c + edge_slot(i)));
 }
 
 // Evaluates queued item `it` (queue qi) in FP64 and folds it into the minimum.
@@ -544,7 +557,7 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
           }
           if (ok) {
             m |= 1u << i;
-            ub = fminf(ub, re_hi(P + re_in(sh.sf[j][i])));
+            ub = fminf(ub, re_hi(P + re_len(sh.sf[j][i])));
           }
           sh.pf[j][i] = pf[r][i];
         }
@@ -577,7 +590,7 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
         const double p = __ldcg(d.phi + nb[i]);
         if (__ldcg(d.st + nb[i]) >= ST_NARROW && p > lower) {
           m |= 1u << i;
-          atomicMin(&sh.res[slot], dkey(p + __ldg(d.cgeo + 10 * c + 6 + i)));
+          atomicMin(&sh.res[slot], dkey(p + sqrt(__ldg(d.cgeo + kCgeoStride * c + edge_slot(i)))));
         }
       }
       if (m) ++n_filtered;
@@ -682,7 +695,7 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
         if (in) { slot = sh.cs[j]; m = sh.vm[j]; bhi = funkey(sh.bhi[slot]); }
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
-          const bool need = in && ((m >> i) & 1u) && !(re_lo(re_in(sh.pf[j][i]) + re_in(sh.sf[j][i])) > bhi);
+          const bool need = in && ((m >> i) & 1u) && !(re_lo(re_in(sh.pf[j][i]) + re_len(sh.sf[j][i])) > bhi);
           queue_exact(d, sh, need, 2, i, slot, j, lane);
         }
       }

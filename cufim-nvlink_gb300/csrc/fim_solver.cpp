@@ -48,6 +48,12 @@ struct DevBuf {
     else p = nullptr;
     return e;
   }
+  // keeps the buffer when it already holds count elements
+  cudaError_t reserve(size_t count)
+  {
+    if (p && n >= (count ? count : 1)) return cudaSuccess;
+    return alloc(count);
+  }
   void release()
   {
     if (p) cudaFree(p);
@@ -403,7 +409,7 @@ extern "C" int fim_set_mesh(fim_solver *s, int64_t nV, const double *xyz, int64_
   CUDA_TRY(s, s->cidx.alloc(nC));
   CUDA_TRY(s, s->cptr.alloc(nL + 1));
   CUDA_TRY(s, s->cids.alloc(nC));
-  CUDA_TRY(s, s->cgeo.alloc(10 * nC));
+  CUDA_TRY(s, s->cgeo.alloc((size_t)kCgeoStride * nC));
   CUDA_TRY(s, s->cgf.alloc((size_t)kCgfStride * nC));
   CUDA_TRY(s, s->nptr.alloc(nL + 1));
   CUDA_TRY(s, s->nbr.alloc(nbr.size()));
@@ -468,13 +474,21 @@ extern "C" int fim_set_conduction(fim_solver *s, const double *fib, const double
   if (!s) return set_err(nullptr, FIM_ERR_INVALID_ARGUMENT, "fim_set_conduction: solver is NULL");
   if (!s->have_mesh) return set_err(s, FIM_ERR_NOT_READY, "fim_set_conduction: no mesh");
   if (!fib || !cf || !ct) return set_err(s, FIM_ERR_INVALID_ARGUMENT, "fim_set_conduction: NULL array");
+  // first tet with a bad speed / fibre (parallel scan, then the message of the first)
+  int64_t bad = s->nT;
+#pragma omp parallel for reduction(min : bad) schedule(static)
   for (int64_t e = 0; e < s->nT; ++e) {
+    const bool ok = cf[e] > 0.0 && ct[e] > 0.0 && std::isfinite(cf[e]) && std::isfinite(ct[e]) &&
+                    std::isfinite(fib[3 * e]) && std::isfinite(fib[3 * e + 1]) && std::isfinite(fib[3 * e + 2]);
+    if (!ok && e < bad) bad = e;
+  }
+  if (bad < s->nT) {
+    const int64_t e = bad;
     if (!(cf[e] > 0.0) || !(ct[e] > 0.0) || !std::isfinite(cf[e]) || !std::isfinite(ct[e]))
       return set_err(s, FIM_ERR_INVALID_ARGUMENT, "fim_set_conduction: tet %lld has speed cf=%g ct=%g",
                      (long long)e, cf[e], ct[e]);
-    if (!std::isfinite(fib[3 * e]) || !std::isfinite(fib[3 * e + 1]) || !std::isfinite(fib[3 * e + 2]))
-      return set_err(s, FIM_ERR_INVALID_ARGUMENT, "fim_set_conduction: tet %lld has a non-finite fibre",
-                     (long long)e);
+    return set_err(s, FIM_ERR_INVALID_ARGUMENT, "fim_set_conduction: tet %lld has a non-finite fibre",
+                   (long long)e);
   }
   CUDA_TRY(s, cudaSetDevice(s->device));
   CUDA_TRY(s, cudaMemcpyAsync(s->fib.p, fib, sizeof(double) * 3 * s->nT, cudaMemcpyHostToDevice, s->stream));
@@ -531,8 +545,8 @@ extern "C" int fim_set_stimuli(fim_solver *s, int64_t n, const int64_t *vertices
     first.erase(it);
   }
   CUDA_TRY(s, cudaSetDevice(s->device));
-  CUDA_TRY(s, s->seed_v.alloc(v.size()));
-  CUDA_TRY(s, s->seed_t.alloc(t.size()));
+  CUDA_TRY(s, s->seed_v.reserve(v.size()));
+  CUDA_TRY(s, s->seed_t.reserve(t.size()));
   if (!v.empty()) {
     CUDA_TRY(s, cudaMemcpyAsync(s->seed_v.p, v.data(), sizeof(int32_t) * v.size(), cudaMemcpyHostToDevice, s->stream));
     CUDA_TRY(s, cudaMemcpyAsync(s->seed_t.p, t.data(), sizeof(double) * t.size(), cudaMemcpyHostToDevice, s->stream));
@@ -637,9 +651,10 @@ extern "C" int fim_get_stats(const fim_solver *s, fim_stats *out)
 // allocation-free re-solve (no counterpart in the reference)
 //
 // Meant for callers that re-solve one staged mesh for many stimulus sets from
-// a loop sharing the device with other work: fim_set_stimuli replaces its
-// seed buffers (cudaFree, which waits for the whole device, then cudaMalloc,
-// which can fail once the caller's own pool holds the free memory).  Here the
+// a loop sharing the device with other work: fim_set_stimuli grows its seed
+// buffers whenever a stimulus set is larger than all before it (cudaFree,
+// which waits for the whole device, then cudaMalloc, which can fail once the
+// caller's own pool holds the free memory).  Here the
 // stimuli and the solve's working set go to the fixed scratch of
 // fim_static.cu, the result to the caller's device buffer; the solver's own
 // buffers and last results are left as they were.

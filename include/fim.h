@@ -139,8 +139,10 @@ int fim_get_stats(const fim_solver *s, fim_stats *out);
  * It calls no allocator: the solve's working set lives in a fixed device
  * array of the library (about 8 MB per device), for callers that must not
  * allocate between solves -- e.g. a loop re-solving one mesh for many
- * stimulus sets while other streams run, where fim_set_stimuli's
- * cudaFree would wait for the whole device.  Limits: at most 131072 mesh
+ * stimulus sets while other streams run, where fim_set_stimuli grows its
+ * seed buffers whenever a stimulus set is larger than all before it (a
+ * cudaFree that waits for the whole device, then a cudaMalloc that can fail
+ * once the caller's own pool holds the memory).  Limits: at most 131072 mesh
  * vertices and 131072 vertex copies (one per submesh holding a vertex),
  * 8192 stimulus entries, 32768 stimulus vertex copies; larger inputs are
  * rejected with FIM_ERR_INVALID_ARGUMENT.  The solver's own buffers, stats
