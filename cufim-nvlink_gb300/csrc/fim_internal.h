@@ -30,8 +30,8 @@ struct FimCtl {
   int32_t n_narrow[3];      // narrow list length of the iteration using this slot
   int32_t n_frozen[3];      // vertices frozen in that iteration
   int32_t n_marked[3];      // neighbours re-solved in that iteration
-  uint32_t bar_count;       // grid barrier arrivals
-  uint32_t bar_gen;         // grid barrier generation
+  uint32_t bar_count;       // grid barrier arrival word (its top bit flips at every barrier)
+  uint32_t bar_pad;
   int32_t error;            // KERR_*
   int32_t error_where;      // phase that failed
   int64_t iterations;

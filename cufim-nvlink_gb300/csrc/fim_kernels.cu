@@ -210,47 +210,39 @@ __device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t *p)
   return v;
 }
 
-__device__ __forceinline__ void st_release_u32(uint32_t *p, uint32_t v)
-{
-  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
-
 __device__ __forceinline__ int ld_volatile_i32(const int32_t *p)
 {
   return *(const volatile int32_t *)p;
 }
 
-// All blocks of the (co-resident) grid meet here.  Every wait is bounded by
-// timeout_ns of %globaltimer and by a spin cap; on expiry the block records
-// KERR_TIMEOUT and the phase, and every block leaves the kernel at its next
-// barrier.  Returns false when the caller must return.
+// All blocks of the (co-resident) grid meet here.  One arrival word: block 0
+// adds 2^31 - (nblocks - 1), every other block adds 1, so the top bit flips
+// exactly when the last block arrives (and the low bits return to zero);
+// everyone waits for the flip.  A block cannot be two flips behind, since the
+// next flip needs its own arrival.  Every wait is bounded by timeout_ns of
+// %globaltimer and by a spin cap; on expiry the block records KERR_TIMEOUT
+// and the phase, and every block leaves the kernel at its next barrier.
+// Returns false when the caller must return.
 __device__ bool grid_sync(FimCtl *ctl, uint32_t nblocks, uint64_t timeout_ns, int where)
 {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
     int ok = 1;
-    const uint32_t gen = ld_acquire_u32(&ctl->bar_gen);
+    const uint32_t inc = blockIdx.x == 0 ? 0x80000000u - (nblocks - 1u) : 1u;
     __threadfence();
-    const uint32_t arrived = atomicAdd(&ctl->bar_count, 1u) + 1u;
-    if (arrived == nblocks) {
-      atomicExch(&ctl->bar_count, 0u);
-      __threadfence();
-      st_release_u32(&ctl->bar_gen, gen + 1u);
-    } else {
-      const uint64_t t0 = global_timer();
-      uint32_t spins = 0;
-      while (ld_acquire_u32(&ctl->bar_gen) == gen) {
-        ++spins;
-        if ((spins & 63u) == 0u) {
-          if (ld_volatile_i32(&ctl->error) != KERR_NONE) { ok = 0; break; }
-          if (global_timer() - t0 > timeout_ns || spins > (1u << 30)) {
-            if (atomicCAS(&ctl->error, KERR_NONE, KERR_TIMEOUT) == KERR_NONE) ctl->error_where = where;
-            ok = 0;
-            break;
-          }
+    const uint32_t old = atomicAdd(&ctl->bar_count, inc);
+    const uint64_t t0 = global_timer();
+    uint32_t spins = 0;
+    while (((ld_acquire_u32(&ctl->bar_count) ^ old) & 0x80000000u) == 0u) {
+      ++spins;
+      if ((spins & 255u) == 0u) {
+        if (ld_volatile_i32(&ctl->error) != KERR_NONE) { ok = 0; break; }
+        if (global_timer() - t0 > timeout_ns || spins > (1u << 30)) {
+          if (atomicCAS(&ctl->error, KERR_NONE, KERR_TIMEOUT) == KERR_NONE) ctl->error_where = where;
+          ok = 0;
+          break;
         }
-        __nanosleep(64);
       }
     }
     if (ok && ld_volatile_i32(&ctl->error) != KERR_NONE) ok = 0;
