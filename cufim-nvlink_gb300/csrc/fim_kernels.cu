@@ -280,10 +280,10 @@ __device__ __forceinline__ double dunkey(unsigned long long k)
 // FP64 pipe for 64 cycles whatever its active lanes, so two blocks per SM
 // would stack their FP64 warps on the same sub-partitions).
 constexpr int kThreads = kSolveThreads;  // threads per block of the solve kernel
-constexpr int kSlots = 64;          // vertices per batch (at most)
-constexpr int kCornerCap = 1536;    // corners per batch
-constexpr int kTriCap = 3 * kCornerCap;  // triangle screens per batch: never full
-constexpr int kTetCap = 1536;       // tet screens per batch
+constexpr int kSlots = 128;         // vertices per batch (at most)
+constexpr int kCornerCap = 2560;    // corners per batch
+constexpr int kTriCap = kCornerCap * 3 / 2;  // triangle screens per batch (more are screened on the spot)
+constexpr int kTetCap = kCornerCap; // tet screens per batch: never full
 constexpr int kQcap = 1024;         // exact solves queued per kind and batch
 
 // Order-preserving map of floats to unsigned integers (for atomicMin).
@@ -313,7 +313,6 @@ struct BatchSh {
   int32_t nb[kCornerCap][3];        // the other three vertices
   float pf[kCornerCap][3];          // their float times
   float sf[kCornerCap][3];          // float edge lengths sqrt(e14), sqrt(e24), sqrt(e34)
-  float gf[kCornerCap][7];          // e13, e23, e34, e12, e14, e24 times 2^-k, and k
   float lbt[kCornerCap][4];         // root-term bounds, then lower bounds of pairs (1,2), (2,3), (1,3) and tet
   uint8_t vm[kCornerCap];           // validity bits of the three neighbours
   uint8_t cs[kCornerCap];           // slot of the corner's vertex
@@ -327,11 +326,11 @@ struct BatchSh {
   int nslot;                        // vertices of the current batch
 };
 
-// Queue item: slot (6 bits) | kind (2 bits) | corner index in the batch (24 bits).
+// Queue item: slot (7 bits) | kind (2 bits) | corner index in the batch (23 bits).
 // kind: triangle pair 0..2 or 3 (tet) in queues 0 and 1, edge 0..2 in queue 2.
 __device__ __forceinline__ uint32_t make_item(int slot, int kind, int j)
 {
-  return (uint32_t)slot | ((uint32_t)kind << 6) | ((uint32_t)j << 8);
+  return (uint32_t)slot | ((uint32_t)kind << 7) | ((uint32_t)j << 9);
 }
 
 // Appends one item per lane with `need` to a list in shared memory
@@ -372,7 +371,7 @@ __device__ __forceinline__ double exact_edge(const FimDev &d, int64_t c, int i, 
 // Evaluates queued item `it` (queue qi) in FP64 and folds it into the minimum.
 __device__ __forceinline__ void run_item(const FimDev &d, BatchSh &sh, int qi, uint32_t it)
 {
-  const int slot = it & 63, kind = (it >> 6) & 3, j = (int)(it >> 8);
+  const int slot = it & 127, kind = (it >> 7) & 3, j = (int)(it >> 9);
   const int64_t c = sh.c0[slot] + (j - sh.cp[slot]);
   const double val = qi == 2 ? exact_edge(d, c, kind, sh.nb[j][kind]) : exact_solve(d, c, kind, sh.nb[j]);
   if (val < FIM_INF) atomicMin(&sh.res[slot], dkey(val));
@@ -390,23 +389,37 @@ __device__ __forceinline__ void queue_exact(const FimDev &d, BatchSh &sh, bool n
   else run_item(d, sh, qi, it);
 }
 
-// FP32 screens of triangle pair k (0: (1,2), 1: (2,3), 2: (1,3)) and of the
-// tet of batch corner j, from the record in shared memory.
-__device__ __forceinline__ CandBound tri_screen_sm(const BatchSh &sh, int j, int k)
+// FP32 screen record of batch corner j: e13, e23, e34, e12, e14, e24 times
+// 2^-k and k (phase A has just read the record, so this hits the caches).
+__device__ __forceinline__ void screen_record(const FimDev &d, const BatchSh &sh, int j, float *g)
 {
-  const float *g = sh.gf[j];
-  const float tk = re_pow2f((int)g[6]);
-  const int i12 = k == 0 ? 3 : (k == 1 ? 1 : 0);   // e12 role
-  const int i13 = k == 0 ? 4 : (k == 1 ? 5 : 4);   // e13 role
-  const int i23 = k == 0 ? 5 : 2;                  // e23 role
-  const int a = k == 0 ? 0 : (k == 1 ? 1 : 0), b = k == 0 ? 1 : 2;
-  return tri_screen(re_scale(re_in(g[i12]), tk), re_scale(re_in(g[i13]), tk), re_scale(re_in(g[i23]), tk),
-                    re_in(sh.pf[j][a]), re_in(sh.pf[j][b]));
+  const int slot = sh.cs[j];
+  const float4 *rp = reinterpret_cast<const float4 *>(d.cgf + kCgfStride * (sh.c0[slot] + (j - sh.cp[slot])));
+  const float4 r0 = __ldg(rp), r1 = __ldg(rp + 1), r2 = __ldg(rp + 2);
+  g[0] = r0.x; g[1] = r0.y; g[2] = r0.z; g[3] = r0.w; g[4] = r1.x; g[5] = r1.y; g[6] = r2.y;
 }
 
-__device__ __forceinline__ CandBound tet_screen_sm(const BatchSh &sh, int j)
+// FP32 screens of triangle pair k (0: (1,2), 1: (2,3), 2: (1,3)) and of the
+// tet of batch corner j.
+__device__ __forceinline__ CandBound tri_screen_sm(const FimDev &d, const BatchSh &sh, int j, int k)
 {
-  const float *g = sh.gf[j];
+  float g[7];
+  screen_record(d, sh, j, g);
+  const float tk = re_pow2f((int)g[6]);
+  // roles e12, e13, e23 of the pair's triangle solve (selects, no indexing)
+  const float g12 = k == 0 ? g[3] : (k == 1 ? g[1] : g[0]);
+  const float g13 = k == 1 ? g[5] : g[4];
+  const float g23 = k == 0 ? g[5] : g[2];
+  const float pa = k == 1 ? sh.pf[j][1] : sh.pf[j][0];
+  const float pb = k == 0 ? sh.pf[j][1] : sh.pf[j][2];
+  return tri_screen(re_scale(re_in(g12), tk), re_scale(re_in(g13), tk), re_scale(re_in(g23), tk), re_in(pa),
+                    re_in(pb));
+}
+
+__device__ __forceinline__ CandBound tet_screen_sm(const FimDev &d, const BatchSh &sh, int j)
+{
+  float g[7];
+  screen_record(d, sh, j, g);
   const Re gs[6] = {re_in(g[0]), re_in(g[1]), re_in(g[2]), re_in(g[3]), re_in(g[4]), re_in(g[5])};
   return tet_screen(gs, re_in(sh.pf[j][0]), re_in(sh.pf[j][1]), re_in(sh.pf[j][2]), (int)g[6]);
 }
@@ -444,7 +457,7 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
                              float lower_lo, float lower_hi, double phi_start, double dt, bool exact_all, int s,
                              int64_t &n_filtered, int64_t &n_exact)
 {
-  constexpr int kPer = (kCornerCap + kThreads - 1) / kThreads;  // corners per thread in phase A
+  constexpr int kPer = 3;  // corners per thread and group in phase A
   const int tid = threadIdx.x, lane = tid & 31;
   const int64_t per_block = ((int64_t)n + gridDim.x - 1) / gridDim.x;
   const int64_t lbeg = min((int64_t)n, (int64_t)blockIdx.x * per_block);
@@ -469,20 +482,24 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
     }
     __syncthreads();
     if (tid < 32) {
-      // inclusive prefix of the corner counts (slots lane and lane + 32)
-      int a = tid < cand ? sh.cnt[tid] : 0, b = tid + 32 < cand ? sh.cnt[tid + 32] : 0;
+      // inclusive prefix of the corner counts (slot lane + 32 r in round r)
+      // and the longest run of slots with <= kCornerCap corners, at least one
+      int carry = 0, fit = 0;
 #pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const int ua = __shfl_up_sync(FULL_MASK, a, o), ub = __shfl_up_sync(FULL_MASK, b, o);
-        if (tid >= o) { a += ua; b += ub; }
+      for (int r = 0; r < kSlots / 32; ++r) {
+        const int sl = tid + 32 * r;
+        int a = sl < cand ? sh.cnt[sl] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int u = __shfl_up_sync(FULL_MASK, a, o);
+          if (tid >= o) a += u;
+        }
+        a += carry;
+        sh.cp[sl + 1] = a;
+        fit += __popc(__ballot_sync(FULL_MASK, sl < cand && a <= kCornerCap));
+        carry = __shfl_sync(FULL_MASK, a, 31);
       }
-      b += __shfl_sync(FULL_MASK, a, 31);
-      sh.cp[tid + 1] = a;
-      sh.cp[tid + 33] = b;
-      // the longest run of slots with <= kCornerCap corners, at least one
-      const unsigned fa = __ballot_sync(FULL_MASK, tid < cand && a <= kCornerCap);
-      const unsigned fb = __ballot_sync(FULL_MASK, tid + 32 < cand && b <= kCornerCap);
-      if (tid == 0) sh.nslot = max(1, __popc(fa) + __popc(fb));
+      if (tid == 0) sh.nslot = max(1, fit);
     }
     __syncthreads();
     const int nslot = sh.nslot;
@@ -493,11 +510,11 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
     // neighbour ids and float screen record to shared memory, pass 2 loads
     // the neighbours' states and float times; within a pass the loads of a
     // thread's corners are independent, so they are all in flight together.
-    {
+    for (int jb = 0; jb < kept; jb += kPer * kThreads) {
       int slot[kPer];
 #pragma unroll
       for (int r = 0; r < kPer; ++r) {
-        const int j = tid + r * kThreads;
+        const int j = jb + tid + r * kThreads;
         slot[r] = 0;
         if (j < kept) {
           int lo = 0, hi = nslot - 1;  // last slot with cp[slot] <= j
@@ -509,12 +526,10 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
           const int64_t c = sh.c0[lo] + (j - sh.cp[lo]);
           const int4 id = __ldg(d.cids + c);
           const float4 *rp = reinterpret_cast<const float4 *>(d.cgf + kCgfStride * c);
-          const float4 r0 = __ldg(rp), r1 = __ldg(rp + 1), r2 = __ldg(rp + 2), r3 = __ldg(rp + 3);
+          const float4 r1 = __ldg(rp + 1), r2 = __ldg(rp + 2), r3 = __ldg(rp + 3);
           sh.lbt[j][0] = r3.x; sh.lbt[j][1] = r3.y; sh.lbt[j][2] = r3.z; sh.lbt[j][3] = r3.w;
           sh.nb[j][0] = id.x; sh.nb[j][1] = id.y; sh.nb[j][2] = id.z;
           sh.sf[j][0] = r1.z; sh.sf[j][1] = r1.w; sh.sf[j][2] = r2.x;
-          sh.gf[j][0] = r0.x; sh.gf[j][1] = r0.y; sh.gf[j][2] = r0.z; sh.gf[j][3] = r0.w;
-          sh.gf[j][4] = r1.x; sh.gf[j][5] = r1.y; sh.gf[j][6] = r2.y;
           sh.cs[j] = (uint8_t)lo;
         }
       }
@@ -522,7 +537,7 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
       uint8_t stn[kPer][3];
 #pragma unroll
       for (int r = 0; r < kPer; ++r) {
-        const int j = tid + r * kThreads;
+        const int j = jb + tid + r * kThreads;
         if (j < kept) {
 #pragma unroll
           for (int i = 0; i < 3; ++i) {
@@ -534,7 +549,7 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
       }
 #pragma unroll
       for (int r = 0; r < kPer; ++r) {
-        const int j = tid + r * kThreads;
+        const int j = jb + tid + r * kThreads;
         if (j >= kept) continue;
         uint32_t m = 0;
         float ub = INFINITY;
@@ -621,7 +636,7 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
           } else {  // list full: screen here
             CandBound cb;
             if (exact_all) { cb.some = CAND_SOME; cb.lb = NAN; cb.ub = INFINITY; }
-            else cb = tri_screen_sm(sh, j, k);
+            else cb = tri_screen_sm(d, sh, j, k);
             if (cb.some && !(cb.lb > bhi)) run_item(d, sh, 1, make_item(slot, k, j));
           }
         }
@@ -644,7 +659,7 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
           const int j = (int)sh.tet[i];
           CandBound cb;
           if (exact_all) { cb.some = CAND_SOME; cb.lb = NAN; cb.ub = INFINITY; }
-          else cb = tet_screen_sm(sh, j);
+          else cb = tet_screen_sm(d, sh, j);
           sh.tet_lb[i] = !cb.some ? NAN : (isnan(cb.lb) ? -INFINITY : cb.lb);
           if (!exact_all && cb.some && cb.ub < INFINITY) atomicMin(&sh.bhi[sh.cs[j]], fkey(cb.ub));
         } else if (i >= tri0) {
@@ -652,7 +667,7 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
           const int j = (int)(sh.tri[t] & 0xffffu), k = (int)(sh.tri[t] >> 16);
           CandBound cb;
           if (exact_all) { cb.some = CAND_SOME; cb.lb = NAN; cb.ub = INFINITY; }
-          else cb = tri_screen_sm(sh, j, k);
+          else cb = tri_screen_sm(d, sh, j, k);
           sh.tri_lb[t] = !cb.some ? NAN : (isnan(cb.lb) ? -INFINITY : cb.lb);
           if (!exact_all && cb.some && cb.ub < INFINITY) atomicMin(&sh.bhi[sh.cs[j]], fkey(cb.ub));
         }
