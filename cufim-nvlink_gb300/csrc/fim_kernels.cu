@@ -316,12 +316,11 @@ struct BatchSh {
   float lbt[kCornerCap][4];         // root-term bounds, then lower bounds of pairs (1,2), (2,3), (1,3) and tet
   uint8_t vm[kCornerCap];           // validity bits of the three neighbours
   uint8_t cs[kCornerCap];           // slot of the corner's vertex
-  // compacted screen lists: item (corner j | pair k << 16) and lower bound
+  // compacted screen lists: item (corner j | pair k << 16)
   uint32_t tri[kTriCap];
-  float tri_lb[kTriCap];
   uint32_t tet[kTetCap];
-  float tet_lb[kTetCap];
   uint32_t q[3][kQcap];             // queued exact solves: [0] tets, [1] triangles, [2] edges
+  float qlb[3][kQcap];              // their lower bounds (rechecked against the final bhi)
   int ntri, ntet, nq[3];
   int nslot;                        // vertices of the current batch
 };
@@ -377,15 +376,16 @@ __device__ __forceinline__ void run_item(const FimDev &d, BatchSh &sh, int qi, u
   if (val < FIM_INF) atomicMin(&sh.res[slot], dkey(val));
 }
 
-// Queues an exact solve (or runs it on the spot when the queue is full).  qi
-// must be the same on every lane of the warp; the item's kind may differ.
+// Queues an exact solve with lower bound lb (or runs it on the spot when the
+// queue is full).  qi must be the same on every lane of the warp; the item's
+// kind may differ.
 __device__ __forceinline__ void queue_exact(const FimDev &d, BatchSh &sh, bool need, int qi, int kind, int slot, int j,
-                                            int lane)
+                                            float lb, int lane)
 {
   const int pos = warp_append(&sh.nq[qi], need, lane);
   if (pos < 0) return;
   const uint32_t it = make_item(slot, kind, j);
-  if (pos < kQcap) sh.q[qi][pos] = it;
+  if (pos < kQcap) { sh.q[qi][pos] = it; sh.qlb[qi][pos] = lb; }
   else run_item(d, sh, qi, it);
 }
 
@@ -443,9 +443,10 @@ __device__ __forceinline__ void set_phi(const FimDev &d, int64_t v, double x)
 //       <= bhi are appended to compacted screen lists (warp ballots);
 //  S -- the screens run over the lists with full warps (triangles and tets
 //       on separate warps); certain upper bounds tighten bhi;
-//  C -- solves and edges whose lower bound does not exceed bhi are queued;
-//  D -- the queued solves run in FP64 (tets, triangles and edges each from a
-//       warp boundary);
+//       a solve whose lower bound does not exceed the current bhi is queued
+//       at once, and so are the edges that can still be the minimum;
+//  D -- the queued solves whose lower bound does not exceed the final bhi run
+//       in FP64 (tets, triangles and edges each from a warp boundary);
 //  E -- the reference's per-vertex decision on the exact minimum:
 //   mode 0 -- narrow vertices: window test (next), freeze test
 //             (cuda_fim.cu:2125-2163);
@@ -649,50 +650,33 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
     }
     __syncthreads();
 
-    // S: screens over the compacted lists; tets from thread 0, triangles from
-    // the next warp boundary
+    // S: screens over the compacted lists (tets from thread 0, triangles from
+    // the next warp boundary, so that every warp holds one kind); a solve
+    // whose lower bound does not exceed the current bhi is queued at once
+    // (bhi only decreases: phase D rechecks against the final bound)
     {
       const int ntet = min(sh.ntet, kTetCap), ntri = min(sh.ntri, kTriCap);
       const int tri0 = (ntet + 31) & ~31;
-      for (int i = tid; i < tri0 + ntri; i += kThreads) {
-        if (i < ntet) {
-          const int j = (int)sh.tet[i];
-          CandBound cb;
-          if (exact_all) { cb.some = CAND_SOME; cb.lb = NAN; cb.ub = INFINITY; }
-          else cb = tet_screen_sm(d, sh, j);
-          sh.tet_lb[i] = !cb.some ? NAN : (isnan(cb.lb) ? -INFINITY : cb.lb);
-          if (!exact_all && cb.some && cb.ub < INFINITY) atomicMin(&sh.bhi[sh.cs[j]], fkey(cb.ub));
-        } else if (i >= tri0) {
-          const int t = i - tri0;
-          const int j = (int)(sh.tri[t] & 0xffffu), k = (int)(sh.tri[t] >> 16);
-          CandBound cb;
-          if (exact_all) { cb.some = CAND_SOME; cb.lb = NAN; cb.ub = INFINITY; }
-          else cb = tri_screen_sm(d, sh, j, k);
-          sh.tri_lb[t] = !cb.some ? NAN : (isnan(cb.lb) ? -INFINITY : cb.lb);
-          if (!exact_all && cb.some && cb.ub < INFINITY) atomicMin(&sh.bhi[sh.cs[j]], fkey(cb.ub));
-        }
-      }
-    }
-    __syncthreads();
-
-    // C: queue the solves and edges that can still be the minimum
-    {
-      const int ntet = min(sh.ntet, kTetCap), ntri = min(sh.ntri, kTriCap);
-      for (int ib = 0; ib < ntet + ntri; ib += kThreads) {
+      for (int ib = 0; ib < tri0 + ntri; ib += kThreads) {
         const int i = ib + tid;
+        const int qi = ib + (tid & ~31) < tri0 ? 0 : 1;  // the same on every lane of the warp
         bool need = false;
         int kind = 0, slot = 0, j = 0;
-        if (i < ntet + ntri) {
-          float l;
-          if (i < ntet) { j = (int)sh.tet[i]; kind = 3; l = sh.tet_lb[i]; }
-          else { const uint32_t it = sh.tri[i - ntet]; j = (int)(it & 0xffffu); kind = (int)(it >> 16); l = sh.tri_lb[i - ntet]; }
+        float lb = 0.f;
+        if (qi == 0 ? i < ntet : i < tri0 + ntri) {
+          if (qi == 0) { j = (int)sh.tet[i]; kind = 3; }
+          else { const uint32_t it = sh.tri[i - tri0]; j = (int)(it & 0xffffu); kind = (int)(it >> 16); }
           slot = sh.cs[j];
-          need = l <= funkey(sh.bhi[slot]);  // NaN (no value) never
+          CandBound cb;
+          if (exact_all) { cb.some = CAND_SOME; cb.lb = NAN; cb.ub = INFINITY; }
+          else cb = qi == 0 ? tet_screen_sm(d, sh, j) : tri_screen_sm(d, sh, j, kind);
+          if (!exact_all && cb.some && cb.ub < INFINITY) atomicMin(&sh.bhi[slot], fkey(cb.ub));
+          lb = isnan(cb.lb) ? -INFINITY : cb.lb;
+          need = cb.some && !(lb > funkey(sh.bhi[slot]));
         }
-        // separate ballots per queue keep each queue warp-compacted
-        queue_exact(d, sh, need && kind == 3, 0, kind, slot, j, lane);
-        queue_exact(d, sh, need && kind != 3, 1, kind, slot, j, lane);
+        queue_exact(d, sh, need, qi, kind, slot, j, lb, lane);
       }
+      // then the edges that can still be the minimum
       for (int jb = 0; jb < kept; jb += kThreads) {
         const int j = jb + tid;
         const bool in = j < kept;
@@ -702,8 +686,9 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
         if (in) { slot = sh.cs[j]; m = sh.vm[j]; bhi = funkey(sh.bhi[slot]); }
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
-          const bool need = in && ((m >> i) & 1u) && !(re_lo(re_in(sh.pf[j][i]) + re_len(sh.sf[j][i])) > bhi);
-          queue_exact(d, sh, need, 2, i, slot, j, lane);
+          const float le = in ? re_lo(re_in(sh.pf[j][i]) + re_len(sh.sf[j][i])) : 0.f;
+          const bool need = in && ((m >> i) & 1u) && !(le > bhi);
+          queue_exact(d, sh, need, 2, i, slot, j, le, lane);
         }
       }
     }
@@ -716,9 +701,15 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
       const int tri0 = (ntet + 31) & ~31;
       const int edge0 = tri0 + ((ntri + 31) & ~31);
       for (int j = tid; j < edge0 + nedge; j += kThreads) {
-        if (j < ntet) { run_item(d, sh, 0, sh.q[0][j]); ++n_exact; }
-        else if (j >= tri0 && j < tri0 + ntri) { run_item(d, sh, 1, sh.q[1][j - tri0]); ++n_exact; }
-        else if (j >= edge0) run_item(d, sh, 2, sh.q[2][j - edge0]);
+        int qi, pos;
+        if (j < ntet) { qi = 0; pos = j; }
+        else if (j >= tri0 && j < tri0 + ntri) { qi = 1; pos = j - tri0; }
+        else if (j >= edge0) { qi = 2; pos = j - edge0; }
+        else continue;
+        const uint32_t it = sh.q[qi][pos];
+        if (sh.qlb[qi][pos] > funkey(sh.bhi[it & 127])) continue;  // overtaken by a later bound
+        run_item(d, sh, qi, it);
+        if (qi < 2) ++n_exact;
       }
     }
     __syncthreads();
