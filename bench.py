@@ -40,7 +40,11 @@ SLAB_CELLS = (266, 93, 40)
 # from ncu dram__bytes_read.sum + dram__bytes_write.sum on this workload
 # (6.110 GB for 4,689,493 vertex updates; profiles/fim_solve_kernel_slab266x93x40_launches.md)
 NCU_DRAM_BYTES_PER_VERTEX_UPDATE = 6.110e9 / 4689493
-METRIC = "slab solves/s (1.03M-vertex anisotropic FIM, bit-exact vs FP64 oracle)"
+METRICS = {
+    "slab": "slab solves/s (1.03M-vertex anisotropic FIM, bit-exact vs FP64 oracle)",
+    "cube": "cube solves/s (9,261-vertex plain FIM, bit-exact vs FP64 oracle)",
+    "shell": "shell solves/s (4.2M-vertex ventricle-like shell FIM, bit-exact vs FP64 oracle)",
+}
 UNIT = "solves/s"
 
 
@@ -50,6 +54,9 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["mine", "reference"], default="mine")
+    ap.add_argument("--workload", choices=["slab", "cube", "shell"], default="slab",
+                    help="slab: 1M-vertex anisotropic slab (default); cube: 9,261-vertex unit cube, isotropic; "
+                         "shell: 4.2M-vertex ventricle-like shell")
     ap.add_argument("--cells", type=str, default=None, help="override slab cells, e.g. 66,23,10")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=None)
@@ -58,6 +65,22 @@ def parse_args():
 
 def workload(args):
     import fim_mesh
+    if args.workload == "cube":
+        case = fim_mesh.cube_case(20)
+        nV, nT = case["xyz"].shape[0], case["tets"].shape[0]
+        return case, {"workload": (f"unit cube, 20^3 Kuhn cells ({nV} vertices, {nT} tets), +-0.2h jitter, "
+                                   "isotropic 0.6 mm/ms, one stimulus at (0,0,0) t0 = 0; one endless window"),
+                      "vertices": nV, "tets": nT, "seed": 1, "l2": "inputs smaller than L2; L2 not flushed",
+                      "parallelism": "replicas"}
+    if args.workload == "shell":
+        case = fim_mesh.shell_case()
+        nV, nT = case["xyz"].shape[0], case["tets"].shape[0]
+        return case, {"workload": (f"ventricle-like shell: prolate spheroid wall 20/20/50 -> 30/30/60 mm, base cut at "
+                                   f"2/3 height, 21x630x321 structured Kuhn grid ({nV} vertices, {nT} tets), "
+                                   "+-0.2h jitter, transmural fibres -60..+60 deg, cf 0.6 / ct 0.24 mm/ms, 8 "
+                                   "endocardial stimuli t0~U[0,15] ms; one endless window"),
+                      "vertices": nV, "tets": nT, "seed": 5, "l2": "inputs larger than L2",
+                      "parallelism": "replicas"}
     cells = tuple(int(x) for x in args.cells.split(",")) if args.cells else SLAB_CELLS
     case = fim_mesh.slab_case(cells=cells)
     nV, nT = case["xyz"].shape[0], case["tets"].shape[0]
@@ -272,12 +295,12 @@ def run_mine(args):
         s.close()
         return
     b_vu = 40.0 * nT / nV + 9.0
-    cells_default = args.cells is None
+    cells_default = args.cells is None and args.workload == "slab"
     upd = stats["vertex_updates"]
     mean_solve_ms = float(np.mean(solve_ms))
     achieved = upd * b_vu / (mean_solve_ms * 1e-3) / 1e9
     out = {
-        "metric": METRIC, "value": world * args.steps / (max_ms * 1e-3), "unit": UNIT, "n_gpus": world,
+        "metric": METRICS[args.workload], "value": world * args.steps / (max_ms * 1e-3), "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": max_ms / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded slab mesh, conduction field and stimuli)", "config": cfg,
@@ -326,7 +349,7 @@ def run_reference(args):
     value = args.steps / t
     cores = os.cpu_count()
     print(json.dumps({
-        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "impl": "reference", "metric": METRICS[args.workload], "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded slab mesh, conduction field and stimuli)", "config": cfg,

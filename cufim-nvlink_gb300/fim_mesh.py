@@ -139,3 +139,82 @@ def batch_cases(n_meshes=32, n_solves=256, vmin=10_000, vmax=500_000, seed=3, ji
         st = rng.uniform(0.0, 10.0, size=ns)
         solves.append(dict(mesh=m, fib=fib, cf=np.full(nT, cf), ct=np.full(nT, ct), seed_v=sv, seed_t=st))
     return meshes, solves
+
+
+def _kuhn_grid_tets(n0, n1, n2, periodic1):
+    """Kuhn tets of an n0 x n1 x n2 grid of cells over (n0+1) x m1 x (n2+1)
+    vertices, vertex (i, j, k) -> i + (n0+1) * (j + m1 * k); with periodic1
+    the second index wraps (m1 = n1), else m1 = n1 + 1."""
+    m1 = n1 if periodic1 else n1 + 1
+
+    def vid(i, j, k):
+        return i + (n0 + 1) * ((j % m1) + m1 * k)
+
+    ci, cj, ck = np.meshgrid(np.arange(n0), np.arange(n1), np.arange(n2), indexing="ij")
+    ci, cj, ck = ci.ravel(order="F"), cj.ravel(order="F"), ck.ravel(order="F")
+    tets = []
+    for path in _KUHN_PATHS:
+        corner = [np.zeros(3, dtype=np.int64)]
+        c = np.zeros(3, dtype=np.int64)
+        for ax in path:
+            c = c.copy()
+            c[ax] = 1
+            corner.append(c)
+        tets.append(np.stack([vid(ci + cc[0], cj + cc[1], ck + cc[2]) for cc in corner], axis=1))
+    return np.stack(tets, axis=1).reshape(-1, 4).astype(np.int32)
+
+
+def shell_case(n_wall=20, n_circ=630, n_long=320, inner=(20.0, 50.0), outer=(30.0, 60.0), apex_hole_deg=3.0,
+               jitter=0.2, seed=5, cf=0.6, ct=0.24, angle=60.0, n_stim=8, t0_max=15.0):
+    """Ventricle-like shell: the wall between two confocal-free prolate
+    spheroids (inner semi-axes 20/20/50 mm, outer 30/30/60 mm, so a 10 mm
+    wall), base cut at z = c/3 (2/3 of the height from the apex), a small
+    hole at the apex instead of a degenerate pole.  Structured transmural x
+    circumferential (periodic) x meridional grid cut into Kuhn tets; defaults
+    give 21 x 630 x 321 = 4,246,830 vertices and 24,192,000 tets.  Fibres in
+    the wall's tangent plane rotate transmurally from -angle (endocardium) to
+    +angle (epicardium) against the circumferential direction; n_stim
+    endocardial stimuli with t0 ~ U[0, t0_max]."""
+    s = np.linspace(0.0, 1.0, n_wall + 1)
+    phi = np.arange(n_circ) * (2 * math.pi / n_circ)
+    t = np.linspace(0.0, 1.0, n_long + 1)
+    S, P, T = np.meshgrid(s, phi, t, indexing="ij")          # (wall, circ, long)
+    a = inner[0] + (outer[0] - inner[0]) * S
+    c = inner[1] + (outer[1] - inner[1]) * S
+    z_cut = outer[1] / 3.0
+    th_base = np.arccos(np.clip(z_cut / c, -1.0, 1.0))
+    th_apex = math.pi - math.radians(apex_hole_deg)
+    if jitter > 0:
+        rng = np.random.default_rng(seed)
+        inner_pts = (S > 0) & (S < 1) & (T > 0) & (T < 1)
+        S = S + np.where(inner_pts, rng.uniform(-jitter, jitter, S.shape) / n_wall, 0.0)
+        P = P + rng.uniform(-jitter, jitter, P.shape) * (2 * math.pi / n_circ)
+        T = T + np.where(inner_pts, rng.uniform(-jitter, jitter, T.shape) / n_long, 0.0)
+        a = inner[0] + (outer[0] - inner[0]) * S
+        c = inner[1] + (outer[1] - inner[1]) * S
+        th_base = np.arccos(np.clip(z_cut / c, -1.0, 1.0))
+    TH = th_base + T * (th_apex - th_base)
+    xyz = np.stack([a * np.sin(TH) * np.cos(P), a * np.sin(TH) * np.sin(P), c * np.cos(TH)], axis=-1)
+    # vertex order of _kuhn_grid_tets: i (wall) fastest, then circ, then long
+    xyz = np.ascontiguousarray(xyz.transpose(2, 1, 0, 3).reshape(-1, 3))
+    tets = _kuhn_grid_tets(n_wall, n_circ, n_long, periodic1=True)
+    # fibre per tet from the centroid's wall depth and tangent frame
+    sv = np.ascontiguousarray(S.transpose(2, 1, 0).reshape(-1))
+    pv = np.ascontiguousarray(P.transpose(2, 1, 0).reshape(-1))
+    thv = np.ascontiguousarray(TH.transpose(2, 1, 0).reshape(-1))
+    s_t = sv[tets].mean(axis=1)
+    # circular mean of the angles of the tet's vertices (the seam wraps)
+    p_t = np.arctan2(np.sin(pv[tets]).mean(axis=1), np.cos(pv[tets]).mean(axis=1))
+    th_t = thv[tets].mean(axis=1)
+    e_circ = np.stack([-np.sin(p_t), np.cos(p_t), np.zeros_like(p_t)], axis=1)
+    e_long = np.stack([np.cos(th_t) * np.cos(p_t), np.cos(th_t) * np.sin(p_t), -np.sin(th_t)], axis=1)
+    alpha = np.deg2rad(-angle + 2 * angle * s_t)
+    fib = np.cos(alpha)[:, None] * e_circ + np.sin(alpha)[:, None] * e_long
+    fib /= np.linalg.norm(fib, axis=1)[:, None]
+    nT = tets.shape[0]
+    rng = np.random.default_rng(seed + 1000)
+    endo = np.nonzero(np.abs(sv) < 1e-12)[0]
+    seeds = rng.choice(endo, size=n_stim, replace=False).astype(np.int32)
+    t0 = rng.uniform(0.0, t0_max, size=n_stim)
+    return dict(xyz=xyz, tets=tets, fib=fib, cf=np.full(nT, cf), ct=np.full(nT, ct), seed_v=seeds, seed_t=t0,
+                name=f"shell{n_wall}x{n_circ}x{n_long}")

@@ -28,7 +28,7 @@ world, rank, local, pg = bench.dist_setup(None)
 assert world == 2 and pg is not None
 bench.barrier(pg)
 v = bench.max_over_ranks(pg, 1.5 + rank)
-print("RANK", rank, "MAX", v, flush=True)
+open(os.path.join({out!r}, "rank%d.txt" % rank), "w").write("RANK %d MAX %s" % (rank, v))
 pg.destroy_process_group()
 """
 
@@ -36,14 +36,14 @@ pg.destroy_process_group()
 def test_max_over_ranks_gloo(tmp_path):
     pytest.importorskip("torch")
     w = tmp_path / "w.py"
-    w.write_text(WORKER.format(root=ROOT))
+    w.write_text(WORKER.format(root=ROOT, out=str(tmp_path)))
     env = dict(os.environ, CUDA_VISIBLE_DEVICES="")
     r = subprocess.run([sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node=2",
                         "--master-addr=127.0.0.1", f"--master-port={_free_port()}", str(w)],
                        capture_output=True, text=True, timeout=300, env=env)
     assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
-    lines = [l for l in r.stdout.splitlines() if l.startswith("RANK")]
-    assert sorted(lines) == ["RANK 0 MAX 2.5", "RANK 1 MAX 2.5"]
+    lines = [(tmp_path / f"rank{k}.txt").read_text() for k in range(2)]
+    assert lines == ["RANK 0 MAX 2.5", "RANK 1 MAX 2.5"]
 
 
 def test_reference_arm_rank0_only(tmp_path):

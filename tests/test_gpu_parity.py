@@ -274,3 +274,14 @@ def test_random_metrics_bit_exact(F, O):
     phi, st, _ = F.solve_case(c)
     phi_o, st_o, _, _ = oracle_single(O, c)
     assert_identical(phi, st, phi_o, st_o)
+
+
+def test_shell_bit_exact(F, O):
+    """Scaled-down ventricle-like shell: curved wall, periodic seam, a hole
+    at the apex, transmural fibre rotation, 8 endocardial stimuli."""
+    import fim_mesh
+    c = fim_mesh.shell_case(n_wall=4, n_circ=48, n_long=24)
+    phi, st, stats = F.solve_case(c)
+    phi_o, st_o, it_o, _ = oracle_single(O, c)
+    assert_identical(phi, st, phi_o, st_o)
+    assert stats["iterations"] == it_o
