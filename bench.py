@@ -44,6 +44,7 @@ METRICS = {
     "slab": "slab solves/s (1.03M-vertex anisotropic FIM, bit-exact vs FP64 oracle)",
     "cube": "cube solves/s (9,261-vertex plain FIM, bit-exact vs FP64 oracle)",
     "shell": "shell solves/s (4.2M-vertex ventricle-like shell FIM, bit-exact vs FP64 oracle)",
+    "batch": "batched solves/s (uneven Kuhn boxes, one persistent launch, bit-exact vs FP64 oracle)",
 }
 UNIT = "solves/s"
 
@@ -54,9 +55,11 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["mine", "reference"], default="mine")
-    ap.add_argument("--workload", choices=["slab", "cube", "shell"], default="slab",
+    ap.add_argument("--workload", choices=["slab", "cube", "shell", "batch"], default="slab",
                     help="slab: 1M-vertex anisotropic slab (default); cube: 9,261-vertex unit cube, isotropic; "
-                         "shell: 4.2M-vertex ventricle-like shell")
+                         "shell: 4.2M-vertex ventricle-like shell; batch: many uneven solves in one launch")
+    ap.add_argument("--batch", type=str, default="32,256,10000,500000",
+                    help="batch workload: meshes,solves,min vertices,max vertices")
     ap.add_argument("--cells", type=str, default=None, help="override slab cells, e.g. 66,23,10")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=None)
@@ -359,10 +362,106 @@ def run_reference(args):
     }), flush=True)
 
 
+def batch_workload(args):
+    import fim_mesh
+    nm, ns, vmin, vmax = (int(x) for x in args.batch.split(","))
+    meshes, solves = fim_mesh.batch_cases(n_meshes=nm, n_solves=ns, vmin=vmin, vmax=vmax)
+    probs = []
+    for sv in solves:
+        m = meshes[sv["mesh"]]
+        probs.append(dict(mesh=sv["mesh"], xyz=m["xyz"], tets=m["tets"], fib=sv["fib"], cf=sv["cf"], ct=sv["ct"],
+                          seed_v=sv["seed_v"], seed_t=sv["seed_t"]))
+    nV = sum(p["xyz"].shape[0] for p in probs)
+    nT = sum(p["tets"].shape[0] for p in probs)
+    sizes = [m["xyz"].shape[0] for m in meshes]
+    cfg = {"workload": (f"{ns} solves over {nm} jittered Kuhn boxes of {min(sizes)}-{max(sizes)} vertices "
+                        f"(log-uniform in [{vmin}, {vmax}]); per solve cf~U[0.4,0.8], ct=cf*U[0.3,0.5], fibre "
+                        "rotation +-U[40,70] deg over z, 1-8 surface stimuli t0~U[0,10] ms; one endless window"),
+           "solves": ns, "meshes": nm, "vertices_total": nV, "tets_total": nT, "seed": 3,
+           "l2": "inputs larger than L2", "parallelism": "one persistent launch for all solves"}
+    return meshes, probs, cfg
+
+
+def run_batch(args):
+    """One step = one fim_batch_solve of every problem (the conduction fields
+    are staged once, before the timed region)."""
+    import torch
+    import fim_api
+    torch.cuda.set_device(0)
+    meshes, probs, cfg = batch_workload(args)
+    ns = len(probs)
+    b = fim_api.Batch()
+    for p in probs:
+        b.add(p["xyz"], p["tets"], p["fib"], p["cf"], p["ct"], p["seed_v"], p["seed_t"])
+    for _ in range(max(args.warmup, 0)):
+        b.solve()
+    clocks = ClockSampler(index=0)
+    clocks.start()
+    dev_ms, wall = [], time.perf_counter()
+    for _ in range(args.steps):
+        b.solve()
+        dev_ms.append(b.stats()["solve_ms"])
+    wall = time.perf_counter() - wall
+    clk = clocks.stop()
+    st = b.stats()
+    # the same problems one fim_solve each (the plain cold-start GPU FIM)
+    seq_ms = 0.0
+    with fim_api.Solver() as s:
+        cur = -1
+        for p in probs:
+            if p["mesh"] != cur:
+                s.set_mesh(p["xyz"], p["tets"])
+                cur = p["mesh"]
+            s.set_conduction(p["fib"], p["cf"], p["ct"])
+            s.set_stimuli(p["seed_v"], p["seed_t"])
+            s.solve()
+            seq_ms += s.stats()["solve_ms"]
+    mean_ms = float(np.mean(dev_ms))
+    out = {
+        "metric": METRICS["batch"], "value": ns / (mean_ms * 1e-3), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": mean_ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Kuhn boxes, conduction draws and stimuli)",
+        "config": cfg, "iterations": st["iterations"], "vertex_updates": st["vertex_updates"],
+        "vertex_updates_per_s": st["vertex_updates"] / (mean_ms * 1e-3), "fp64_local_solves": st["exact_evals"],
+        "sequential": {"value": ns / (seq_ms * 1e-3), "unit": UNIT,
+                       "how": "the same problems, one fim_solve each (device time of the solves)"},
+        "speedup_vs_sequential": seq_ms / mean_ms,
+        "e2e": {"value": ns * args.steps / wall, "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": int(12 * cfg["vertices_total"]),
+                "how": "wall time of fim_batch_solve (launch + D2H of every problem's times and states)"},
+        "gpu_launches": args.steps, "clocks": clk,
+    }
+    if not args.no_cpu_baseline:
+        from oracle import oracle as O
+        from oracle import build as obuild
+        obuild.build_oracle()
+        t_cpu, n_cpu, mism = 0.0, 0, 0
+        order = sorted(range(ns), key=lambda i: probs[i]["xyz"].shape[0])
+        for i in order[::max(1, ns // 16)]:
+            p = probs[i]
+            nV = p["xyz"].shape[0]
+            slots, _, _, _ = O.reference_slots(nV, p["tets"], None)
+            t0 = time.perf_counter()
+            geo = O.metric_geo(slots, p["xyz"], p["fib"], p["cf"], p["ct"])
+            phi_o, _, _, _ = O.solve_pure(nV, slots, geo, p["seed_v"], p["seed_t"])
+            t_cpu += time.perf_counter() - t0
+            n_cpu += 1
+            mism += int(np.count_nonzero(b.times(i, with_state=False) != phi_o))
+            if t_cpu > 20.0:
+                break
+        out["cpu_baseline"] = {"value": n_cpu / t_cpu, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+                               "sample": f"{n_cpu} of the {ns} solves (sizes spread), FP64 C oracle, OpenMP"}
+        out["parity"] = {"checked_solves": n_cpu, "n_bit_mismatch": mism}
+    b.close()
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "batch":
+        run_batch(args)
     else:
         run_mine(args)
 

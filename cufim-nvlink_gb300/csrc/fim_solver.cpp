@@ -735,3 +735,166 @@ extern "C" int fim_solve_noalloc(fim_solver *s, int64_t n, const int64_t *vertic
                    (long long)p.max_iter);
   return FIM_OK;
 }
+
+// ---------------------------------------------------------------------------
+// batched solves (no counterpart in the reference)
+//
+// Independent problems are staged as ONE disjoint mesh in an internal
+// solver: every FIM iteration of the persistent kernel advances all of them,
+// so the per-iteration latencies (grid barriers, batch phase chains) are
+// paid once for the whole batch.  A problem's vertices only ever meet its
+// own tets, and with one endless window and start times >= 0 the reference's
+// front-width test never rejects a reached time, so each problem evolves
+// exactly as it would alone (a problem that has converged simply has an
+// empty narrow list).
+
+struct fim_batch {
+  fim_opts opts{};
+  fim_solver *s = nullptr;
+  std::string err;
+  struct Problem {
+    int64_t nV = 0, nT = 0;
+    int64_t v0 = 0;  // first vertex in the union
+  };
+  std::vector<Problem> probs;
+  std::vector<double> xyz, fib, cf, ct, stim_t;
+  std::vector<int64_t> tets, stim_v;
+  bool staged = false, solved = false;
+  std::vector<double> phi;
+  std::vector<int32_t> st;
+};
+
+static int batch_err(fim_batch *b, int code, const char *fmt, ...)
+{
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  if (b) b->err = buf;
+  g_last_error = buf;
+  return code;
+}
+
+extern "C" int fim_batch_create(const fim_opts *opts, fim_batch **out)
+{
+  if (!out) return batch_err(nullptr, FIM_ERR_INVALID_ARGUMENT, "fim_batch_create: out is NULL");
+  *out = nullptr;
+  fim_opts o;
+  if (opts) o = *opts;
+  else fim_default_opts(&o);
+  if ((o.dt > 0.0 && std::isfinite(o.dt)) || o.n_steps != 1)
+    return batch_err(nullptr, FIM_ERR_INVALID_ARGUMENT,
+                     "fim_batch_create: batched solves run one endless window (dt <= 0, n_steps = 1)");
+  fim_batch *b = new (std::nothrow) fim_batch();
+  if (!b) return batch_err(nullptr, FIM_ERR_OUT_OF_MEMORY, "fim_batch_create: out of host memory");
+  b->opts = o;
+  const int rc = fim_create(&o, &b->s);
+  if (rc != FIM_OK) {
+    const std::string m = fim_last_error(nullptr);
+    delete b;
+    return batch_err(nullptr, rc, "fim_batch_create: %s", m.c_str());
+  }
+  *out = b;
+  return FIM_OK;
+}
+
+extern "C" int fim_batch_destroy(fim_batch *b)
+{
+  if (!b) return FIM_OK;
+  fim_destroy(b->s);
+  delete b;
+  return FIM_OK;
+}
+
+extern "C" const char *fim_batch_last_error(const fim_batch *b)
+{
+  return b ? b->err.c_str() : g_last_error.c_str();
+}
+
+extern "C" int fim_batch_add(fim_batch *b, int64_t nV, const double *xyz, int64_t nT, const int64_t *tets,
+                             const double *fib, const double *cf, const double *ct, int64_t n_stim,
+                             const int64_t *stim_v, const double *stim_t, int64_t *problem)
+{
+  if (!b) return batch_err(nullptr, FIM_ERR_INVALID_ARGUMENT, "fim_batch_add: batch is NULL");
+  if (nV <= 0 || nT <= 0 || !xyz || !tets || !fib || !cf || !ct || n_stim < 0 || (n_stim > 0 && (!stim_v || !stim_t)))
+    return batch_err(b, FIM_ERR_INVALID_ARGUMENT, "fim_batch_add: bad size or NULL array");
+  const int64_t v0 = b->probs.empty() ? 0 : b->probs.back().v0 + b->probs.back().nV;
+  if (v0 + nV > INT32_MAX || (int64_t)(b->tets.size() / 4) + nT > INT32_MAX / 4)
+    return batch_err(b, FIM_ERR_INVALID_ARGUMENT, "fim_batch_add: the batch exceeds 2^31 vertices or 2^29 tets");
+  for (int64_t i = 0; i < 4 * nT; ++i)
+    if (tets[i] < 0 || tets[i] >= nV)
+      return batch_err(b, FIM_ERR_INVALID_ARGUMENT, "fim_batch_add: tet %lld refers to vertex %lld outside [0,%lld)",
+                       (long long)(i / 4), (long long)tets[i], (long long)nV);
+  for (int64_t i = 0; i < n_stim; ++i) {
+    if (stim_v[i] < 0 || stim_v[i] >= nV)
+      return batch_err(b, FIM_ERR_INVALID_ARGUMENT, "fim_batch_add: stimulus vertex %lld outside [0,%lld)",
+                       (long long)stim_v[i], (long long)nV);
+    if (!(stim_t[i] >= 0.0) || !std::isfinite(stim_t[i]))
+      return batch_err(b, FIM_ERR_INVALID_ARGUMENT,
+                       "fim_batch_add: start time %lld is %g; batched solves need finite times >= 0", (long long)i,
+                       stim_t[i]);
+  }
+  try {
+    b->xyz.insert(b->xyz.end(), xyz, xyz + 3 * nV);
+    for (int64_t i = 0; i < 4 * nT; ++i) b->tets.push_back(tets[i] + v0);
+    b->fib.insert(b->fib.end(), fib, fib + 3 * nT);
+    b->cf.insert(b->cf.end(), cf, cf + nT);
+    b->ct.insert(b->ct.end(), ct, ct + nT);
+    for (int64_t i = 0; i < n_stim; ++i) { b->stim_v.push_back(stim_v[i] + v0); b->stim_t.push_back(stim_t[i]); }
+    fim_batch::Problem p;
+    p.nV = nV; p.nT = nT; p.v0 = v0;
+    b->probs.push_back(p);
+  } catch (const std::bad_alloc &) {
+    return batch_err(b, FIM_ERR_OUT_OF_MEMORY, "fim_batch_add: out of host memory");
+  }
+  if (problem) *problem = (int64_t)b->probs.size() - 1;
+  b->staged = b->solved = false;
+  return FIM_OK;
+}
+
+extern "C" int fim_batch_solve(fim_batch *b, void *stream)
+{
+  if (!b) return batch_err(nullptr, FIM_ERR_INVALID_ARGUMENT, "fim_batch_solve: batch is NULL");
+  if (b->probs.empty()) return batch_err(b, FIM_ERR_NOT_READY, "fim_batch_solve: no problems added");
+  fim_solver *s = b->s;
+  int rc;
+  if (!b->staged) {
+    const int64_t nV = (int64_t)b->xyz.size() / 3, nT = (int64_t)b->tets.size() / 4;
+    if ((rc = fim_set_mesh(s, nV, b->xyz.data(), nT, b->tets.data(), nullptr)) != FIM_OK ||
+        (rc = fim_set_conduction(s, b->fib.data(), b->cf.data(), b->ct.data())) != FIM_OK ||
+        (rc = fim_set_stimuli(s, (int64_t)b->stim_v.size(), b->stim_v.data(), b->stim_t.data())) != FIM_OK)
+      return batch_err(b, rc, "fim_batch_solve: %s", fim_last_error(s));
+    b->staged = true;
+  }
+  if ((rc = fim_solve(s, stream)) != FIM_OK) return batch_err(b, rc, "fim_batch_solve: %s", fim_last_error(s));
+  try {
+    b->phi.resize(b->xyz.size() / 3);
+    b->st.resize(b->xyz.size() / 3);
+  } catch (const std::bad_alloc &) {
+    return batch_err(b, FIM_ERR_OUT_OF_MEMORY, "fim_batch_solve: out of host memory");
+  }
+  if ((rc = fim_get_times(s, b->phi.data(), b->st.data())) != FIM_OK)
+    return batch_err(b, rc, "fim_batch_solve: %s", fim_last_error(s));
+  b->solved = true;
+  return FIM_OK;
+}
+
+extern "C" int fim_batch_get_times(fim_batch *b, int64_t problem, double *phi, int32_t *state)
+{
+  if (!b) return batch_err(nullptr, FIM_ERR_INVALID_ARGUMENT, "fim_batch_get_times: batch is NULL");
+  if (!b->solved) return batch_err(b, FIM_ERR_NOT_READY, "fim_batch_get_times: no finished solve");
+  if (problem < 0 || problem >= (int64_t)b->probs.size())
+    return batch_err(b, FIM_ERR_INVALID_ARGUMENT, "fim_batch_get_times: problem %lld outside [0,%lld)",
+                     (long long)problem, (long long)b->probs.size());
+  const fim_batch::Problem &p = b->probs[problem];
+  if (phi) std::copy(b->phi.begin() + p.v0, b->phi.begin() + p.v0 + p.nV, phi);
+  if (state) std::copy(b->st.begin() + p.v0, b->st.begin() + p.v0 + p.nV, state);
+  return FIM_OK;
+}
+
+extern "C" int fim_batch_get_stats(const fim_batch *b, fim_stats *out)
+{
+  if (!b || !out) return batch_err(nullptr, FIM_ERR_INVALID_ARGUMENT, "fim_batch_get_stats: NULL argument");
+  return fim_get_stats(b->s, out);
+}

@@ -24,7 +24,9 @@ FAR, NEIG, NARROW, NEXT, FROZEN, TAIL = range(6)
 EXPORTS = ["fim_default_opts", "fim_create", "fim_destroy", "fim_last_error", "fim_set_mesh",
            "fim_set_conduction", "fim_set_conduction_device", "fim_set_stimuli", "fim_solve",
            "fim_get_times", "fim_get_times_device", "fim_get_stats", "fim_vtk_read", "fim_vtk_write",
-           "fim_read_tags", "fim_load_plan", "fim_set_stream", "fim_solve_noalloc"]
+           "fim_read_tags", "fim_load_plan", "fim_set_stream", "fim_solve_noalloc", "fim_batch_create",
+           "fim_batch_destroy", "fim_batch_last_error", "fim_batch_add", "fim_batch_solve", "fim_batch_get_times",
+           "fim_batch_get_stats"]
 
 
 class FimOpts(C.Structure):
@@ -78,6 +80,14 @@ def lib():
         L.fim_get_times_device.argtypes = [vp, vp]
         L.fim_get_stats.argtypes = [vp, P(FimStats)]
         L.fim_solve_noalloc.argtypes = [vp, i64, P(i64), P(d), vp, vp]
+        L.fim_batch_create.argtypes = [P(FimOpts), P(vp)]
+        L.fim_batch_destroy.argtypes = [vp]
+        L.fim_batch_last_error.argtypes = [vp]
+        L.fim_batch_last_error.restype = C.c_char_p
+        L.fim_batch_add.argtypes = [vp, i64, P(d), i64, P(i64), P(d), P(d), P(d), i64, P(i64), P(d), P(i64)]
+        L.fim_batch_solve.argtypes = [vp, vp]
+        L.fim_batch_get_times.argtypes = [vp, i64, P(d), P(i32)]
+        L.fim_batch_get_stats.argtypes = [vp, P(FimStats)]
         L.fim_vtk_read.argtypes = [C.c_char_p, P(i64), P(i64), P(d), P(i64), P(i32)]
         L.fim_vtk_write.argtypes = [C.c_char_p, i64, i64, P(d), P(i64), P(i32), P(d), P(d)]
         L.fim_read_tags.argtypes = [C.c_char_p, P(i64), P(i32)]
@@ -184,6 +194,69 @@ class Solver:
     def stats(self):
         s = FimStats()
         _check(lib().fim_get_stats(self.h, C.byref(s)), self.h)
+        return {k: getattr(s, k) for k, _ in FimStats._fields_}
+
+
+def _bcheck(rc, b):
+    if rc != FIM_OK:
+        msg = lib().fim_batch_last_error(b)
+        raise FimError(rc, msg.decode() if msg else "")
+
+
+class Batch:
+    """Many independent problems solved by one persistent launch (a fim_batch handle)."""
+
+    def __init__(self, **opts):
+        self.h = C.c_void_p()
+        o = default_opts(**opts)
+        _check(lib().fim_batch_create(C.byref(o), C.byref(self.h)))
+        self.sizes = []
+
+    def close(self):
+        if self.h:
+            lib().fim_batch_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def add(self, xyz, tets, fib, cf, ct, seed_v, seed_t):
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+        tets = np.ascontiguousarray(tets, dtype=np.int64)
+        fib = np.ascontiguousarray(fib, dtype=np.float64)
+        cf = np.ascontiguousarray(cf, dtype=np.float64)
+        ct = np.ascontiguousarray(ct, dtype=np.float64)
+        sv = np.ascontiguousarray(seed_v, dtype=np.int64)
+        st = np.ascontiguousarray(seed_t, dtype=np.float64)
+        pid = C.c_int64()
+        _bcheck(lib().fim_batch_add(self.h, xyz.shape[0], _ptr(xyz, C.c_double), tets.shape[0], _ptr(tets, C.c_int64),
+                                    _ptr(fib, C.c_double), _ptr(cf, C.c_double), _ptr(ct, C.c_double), sv.shape[0],
+                                    _ptr(sv, C.c_int64), _ptr(st, C.c_double), C.byref(pid)), self.h)
+        self.sizes.append(xyz.shape[0])
+        return pid.value
+
+    def solve(self, stream=None):
+        _bcheck(lib().fim_batch_solve(self.h, C.c_void_p(stream) if stream else None), self.h)
+
+    def times(self, problem, with_state=True):
+        n = self.sizes[problem]
+        phi = np.empty(n, dtype=np.float64)
+        st = np.empty(n, dtype=np.int32) if with_state else None
+        _bcheck(lib().fim_batch_get_times(self.h, problem, _ptr(phi, C.c_double), _ptr(st, C.c_int32)), self.h)
+        return (phi, st) if with_state else phi
+
+    def stats(self):
+        s = FimStats()
+        _bcheck(lib().fim_batch_get_stats(self.h, C.byref(s)), self.h)
         return {k: getattr(s, k) for k, _ in FimStats._fields_}
 
 

@@ -156,6 +156,32 @@ int fim_get_stats(const fim_solver *s, fim_stats *out);
 int fim_solve_noalloc(fim_solver *s, int64_t n, const int64_t *vertices, const double *t0,
                       double *d_phi, void *stream);
 
+/* Batched solves -- no counterpart in the reference (the benchmark spec's
+ * batching: many solves of uneven size in one persistent launch).
+ * Independent problems (mesh + conduction + stimuli, each with its own
+ * vertex numbering) are staged as one disjoint mesh and solved by ONE launch
+ * of the persistent kernel: every FIM iteration advances all of them.  Each
+ * problem's times are bit-identical to solving it alone with fim_solve.
+ * Batches run one endless window (opts->dt <= 0 or inf, n_steps = 1) and
+ * take start times >= 0, where the front-width rule never fires.  Problems
+ * are copied at fim_batch_add; staging happens at the first fim_batch_solve
+ * after an add.  Errors: fim_batch_last_error(batch). */
+typedef struct fim_batch fim_batch;
+int fim_batch_create(const fim_opts *opts, fim_batch **out);
+int fim_batch_destroy(fim_batch *b);
+const char *fim_batch_last_error(const fim_batch *b);
+/* Adds a problem (host arrays as for fim_set_mesh / fim_set_conduction /
+ * fim_set_stimuli; tets index 0..n_vertices-1) and returns its index. */
+int fim_batch_add(fim_batch *b, int64_t n_vertices, const double *xyz, int64_t n_tets, const int64_t *tets,
+                  const double *fib, const double *cf, const double *ct, int64_t n_stim,
+                  const int64_t *stim_vertices, const double *stim_t0, int64_t *problem);
+/* Solves every problem of the batch (one persistent launch) and waits. */
+int fim_batch_solve(fim_batch *b, void *stream);
+/* Times (and states, or NULL) of one problem after fim_batch_solve. */
+int fim_batch_get_times(fim_batch *b, int64_t problem, double *phi, int32_t *state);
+/* Statistics of the last batch solve (all problems together). */
+int fim_batch_get_stats(const fim_batch *b, fim_stats *out);
+
 /* Reference-compatible files.  fim_vtk_* read/write the legacy ASCII VTK
  * that the reference reads and writes (load_vtk / save_vtk,
  * src/io/vtk.cpp:11-211); fim_read_tags reads a partition file

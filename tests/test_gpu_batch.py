@@ -1,0 +1,70 @@
+"""Batched solves (fim_batch_*): many independent problems of uneven size in
+one persistent launch, each bit-identical to solving it alone and to the
+FP64 oracle."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def F(built_library):
+    import fim_api
+    return fim_api
+
+
+@pytest.fixture(scope="module")
+def O(oracle_lib):
+    return oracle_lib
+
+
+def _problems(n_meshes=6, n_solves=12, vmin=300, vmax=6000, seed=11):
+    import fim_mesh
+    meshes, solves = fim_mesh.batch_cases(n_meshes=n_meshes, n_solves=n_solves, vmin=vmin, vmax=vmax, seed=seed)
+    out = []
+    for sv in solves:
+        m = meshes[sv["mesh"]]
+        out.append(dict(xyz=m["xyz"], tets=m["tets"], fib=sv["fib"], cf=sv["cf"], ct=sv["ct"],
+                        seed_v=sv["seed_v"], seed_t=sv["seed_t"]))
+    return out
+
+
+def test_batch_equals_single_solves(F, O):
+    probs = _problems()
+    with F.Batch() as b:
+        ids = [b.add(p["xyz"], p["tets"], p["fib"], p["cf"], p["ct"], p["seed_v"], p["seed_t"]) for p in probs]
+        b.solve()
+        stats = b.stats()
+        got = [b.times(i) for i in ids]
+        # a second solve of the same batch (staging reused) gives the same times
+        b.solve()
+        again = [b.times(i) for i in ids]
+    for (phi, st), (phi2, st2) in zip(got, again):
+        assert np.array_equal(phi, phi2) and np.array_equal(st, st2)
+    iters = []
+    for p, (phi, st) in zip(probs, got):
+        phi1, st1, s1 = F.solve_case(p)
+        assert np.array_equal(phi, phi1) and np.array_equal(st, st1)
+        iters.append(s1["iterations"])
+    # the batch iterates as long as its slowest problem
+    assert stats["iterations"] == max(iters)
+    # two problems against the oracle as well
+    for p, (phi, st) in list(zip(probs, got))[:2]:
+        nV = p["xyz"].shape[0]
+        slots, _, _, _ = O.reference_slots(nV, p["tets"], None)
+        geo = O.metric_geo(slots, p["xyz"], p["fib"], p["cf"], p["ct"])
+        phi_o, st_o, _, _ = O.solve_pure(nV, slots, geo, p["seed_v"], p["seed_t"])
+        assert np.array_equal(phi, phi_o) and np.array_equal(st, st_o)
+
+
+def test_batch_rejects_windows_and_negative_times(F):
+    with pytest.raises(F.FimError) as e:
+        F.Batch(dt=10.0)
+    assert e.value.code == 1
+    p = _problems(n_meshes=1, n_solves=1)[0]
+    with F.Batch() as b:
+        with pytest.raises(F.FimError) as e:
+            b.add(p["xyz"], p["tets"], p["fib"], p["cf"], p["ct"], p["seed_v"], -np.ones(len(p["seed_v"])))
+        assert e.value.code == 1 and "times >= 0" in str(e.value)
+        with pytest.raises(F.FimError):
+            b.solve()  # nothing added
