@@ -45,6 +45,7 @@ METRICS = {
     "cube": "cube solves/s (9,261-vertex plain FIM, bit-exact vs FP64 oracle)",
     "shell": "shell solves/s (4.2M-vertex ventricle-like shell FIM, bit-exact vs FP64 oracle)",
     "batch": "batched solves/s (uneven Kuhn boxes, one persistent launch, bit-exact vs FP64 oracle)",
+    "warm": "warm-started vs cold FIM solves/s (learned per-vertex start times, slab family)",
 }
 UNIT = "solves/s"
 
@@ -55,9 +56,10 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["mine", "reference"], default="mine")
-    ap.add_argument("--workload", choices=["slab", "cube", "shell", "batch"], default="slab",
+    ap.add_argument("--workload", choices=["slab", "cube", "shell", "batch", "warm"], default="slab",
                     help="slab: 1M-vertex anisotropic slab (default); cube: 9,261-vertex unit cube, isotropic; "
-                         "shell: 4.2M-vertex ventricle-like shell; batch: many uneven solves in one launch")
+                         "shell: 4.2M-vertex ventricle-like shell; batch: many uneven solves in one launch; "
+                         "warm: learned warm start against the cold start")
     ap.add_argument("--batch", type=str, default="32,256,10000,500000",
                     help="batch workload: meshes,solves,min vertices,max vertices")
     ap.add_argument("--cells", type=str, default=None, help="override slab cells, e.g. 66,23,10")
@@ -456,12 +458,66 @@ def run_batch(args):
     print(json.dumps(out), flush=True)
 
 
+def run_warm(args):
+    """Trains the warm-start network on FIM maps of small slabs of the bench
+    family (generated by the solver), then solves held-out maps cold and warm.
+    One step = one held-out map solved once each way."""
+    import torch
+    import fim_api
+    import fim_warm
+    torch.cuda.set_device(0)
+    cells = (66, 23, 10)
+    t0 = time.perf_counter()
+    train_maps = fim_warm.make_maps(400, cells, 7, torch)
+    gen_s = time.perf_counter() - t0
+    test_maps = fim_warm.make_maps(max(args.steps, 1), cells, 8, torch)
+    mlp = fim_api.Mlp(seed=5)
+    t0 = time.perf_counter()
+    losses = fim_warm.train(mlp, train_maps, steps=3000, batch=4096, lr=1e-3, torch=torch)
+    train_s = time.perf_counter() - t0
+    ev = fim_warm.evaluate(mlp, test_maps, torch)
+    cold_ms, warm_ms, cold_it, warm_it, err, below = [], [], [], [], [], []
+    with fim_api.Solver() as s:
+        for m in test_maps:
+            phi, st, start = fim_warm.warm_solve(s, mlp, m, torch)
+            r = m.phi < 1e300
+            tmax = m.phi[r].max()
+            cold_ms.append(m.cold["solve_ms"])
+            warm_ms.append(st["solve_ms"])
+            cold_it.append(m.cold["iterations"])
+            warm_it.append(st["iterations"])
+            err.append(float(np.abs(phi - m.phi)[r].max() / tmax))
+            below.append(float(np.mean(start[r] < m.phi[r])))
+    mlp.close()
+    nv = test_maps[0].nV
+    out = {
+        "metric": METRICS["warm"], "value": len(warm_ms) / (sum(warm_ms) * 1e-3), "unit": UNIT, "n_gpus": 1,
+        "steps": len(warm_ms), "warmup": 0, "ms_per_step": float(np.mean(warm_ms)), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64 solve, bf16 network",
+        "data": "synthetic (FIM maps of seeded slabs generated by the solver)",
+        "config": {"workload": (f"slab family {cells[0]}x{cells[1]}x{cells[2]} Kuhn cells ({nv} vertices), random "
+                                "cf/ct/fibre/scar/stimuli; network 7->128->128->128->1 trained on 400 maps, 3000 "
+                                "Adam steps of 4096 vertices; start = 1.05 x prediction"), "train_maps": 400},
+        "cold": {"value": len(cold_ms) / (sum(cold_ms) * 1e-3), "unit": UNIT, "iterations": float(np.mean(cold_it))},
+        "warm_iterations": float(np.mean(warm_it)),
+        "speedup_vs_cold": sum(cold_ms) / sum(warm_ms),
+        "warm_max_rel_err_vs_cold": max(err), "start_below_cold_frac": float(np.mean(below)),
+        "network": ev, "train_loss_first_last": [float(np.mean(losses[:10])), float(np.mean(losses[-50:]))],
+        "generation_s": gen_s, "training_s": train_s, "gpu_launches": 2 * len(warm_ms),
+        "e2e": {"value": None, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0,
+                "how": "report line; the end-to-end number is the slab workload's"},
+    }
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse_args()
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "batch":
         run_batch(args)
+    elif args.workload == "warm":
+        run_warm(args)
     else:
         run_mine(args)
 

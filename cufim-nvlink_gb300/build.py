@@ -20,7 +20,7 @@ CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SOURCES = ["fim_kernels.cu", "fim_static.cu"]
+CU_SOURCES = ["fim_kernels.cu", "fim_static.cu", "fim_mlp.cu"]
 CPP_SOURCES = ["fim_solver.cpp", "fim_io.cpp", "cuda_solver_fim.cpp"]
 CLI_SOURCES = ["fim_cli.cpp"]
 

@@ -79,6 +79,7 @@ struct FimDev {
   const int32_t *seed_v;
   const double *seed_t;
   int32_t nseed;
+  const double *phi_init;     // warm start per vertex (nullptr: cold start)
   FimCtl *ctl;
 };
 
@@ -107,6 +108,25 @@ cudaError_t launch_solve(const FimDev &d, const FimParams &p, int grid, int bloc
 cudaError_t solve_grid_size(int device, int block, int *grid);
 // Writes phi (any order) into out.
 cudaError_t launch_copy(const double *src, double *dst, int64_t n, cudaStream_t stream);
+
+// ---- learned warm start (fim_mlp.cu) ----
+// Network 7 (padded to kMlpIn) -> kMlpH -> kMlpH -> kMlpH -> 1.  Parameter
+// vector: the three GEMM weight matrices first ([in][out], row-major; their
+// BF16 copies cover exactly this prefix), then b1, b2, b3, w4, b4.
+constexpr int kMlpIn = 64, kMlpH = 128, kMlpFeatures = 7;
+constexpr int kMlpOW1 = 0, kMlpOW2 = kMlpIn * kMlpH, kMlpOW3 = kMlpOW2 + kMlpH * kMlpH;
+constexpr int kMlpW16 = kMlpOW3 + kMlpH * kMlpH;
+constexpr int kMlpOB1 = kMlpW16, kMlpOB2 = kMlpOB1 + kMlpH, kMlpOB3 = kMlpOB2 + kMlpH;
+constexpr int kMlpOW4 = kMlpOB3 + kMlpH, kMlpOB4 = kMlpOW4 + kMlpH;
+constexpr int kMlpParams = kMlpOB4 + 1;
+
+// Feature rows of the learned warm start (fim_mlp.cu); red receives the
+// bounding box and the largest stimulus distance (features_scale reads it).
+cudaError_t launch_features(int nV, int64_t nT, const double *xyz, const int32_t *tslots, const double *fib,
+                            const double *cf, const double *ct, int nseed, const int32_t *seed_v,
+                            const double *seed_t, float *acc, float *dist, unsigned int *red, void *X,
+                            cudaStream_t st);
+float features_scale(const unsigned int *host_red);
 
 // ---- fixed scratch of fim_solve_noalloc (fim_static.cu) ----
 constexpr int64_t kStaticMaxCopies = 131072;       // vertex copies of the mesh

@@ -754,8 +754,10 @@ __global__ void __launch_bounds__(kThreads, 1) fim_solve_kernel(FimDev d, FimPar
   BatchSh &sh = *reinterpret_cast<BatchSh *>(fim_smem);
 
   // reset_states_gpu + update_events_gpu: phi = INF, far; seeds narrow.
+  // (warm start: every vertex narrow at its given time instead)
   for (int64_t v = gtid; v < d.nV; v += nthreads) {
-    set_phi(d, v, FIM_INF); d.phi2[v] = FIM_INF; d.st[v] = ST_FAR; d.tst[v] = ST_FAR; d.flag[v] = 0;
+    const double x = d.phi_init ? d.phi_init[v] : FIM_INF;
+    set_phi(d, v, x); d.phi2[v] = x; d.st[v] = x < FIM_INF ? ST_NARROW : ST_FAR; d.tst[v] = ST_FAR; d.flag[v] = 0;
   }
   // failure-detection test hook: this block never arrives at the barrier (a
   // flag that nothing sets), so the others' bounded waits must expire

@@ -106,6 +106,7 @@ struct fim_solver {
   DevBuf<FimCtl> ctl;
   FimCtl last_ctl{};
   fim_stats stats{};
+  const double *warm = nullptr;  // caller's warm-start times (device) or nullptr
 };
 
 static int set_err(fim_solver *s, int code, const char *fmt, ...)
@@ -397,6 +398,7 @@ extern "C" int fim_set_mesh(fim_solver *s, int64_t nV, const double *xyz, int64_
   s->front_width = 1.01 * std::sqrt(maxe2) / 0.6;
 
   CUDA_TRY(s, cudaSetDevice(s->device));
+  s->warm = nullptr;  // a warm start belongs to the previous mesh
   s->have_mesh = s->have_cond = s->have_stim = s->solved = false;
   s->nV = nV; s->nT = nT; s->nC = nC; s->nL = nL;
   s->n_submeshes = S.n_submeshes;
@@ -574,6 +576,7 @@ extern "C" int fim_solve(fim_solver *s, void *stream)
   d.list[0] = s->list0.p; d.list[1] = s->list1.p; d.list[2] = s->list2.p;
   d.lfrozen = s->lfrozen.p; d.lmarked = s->lmarked.p; d.dec = s->dec.p;
   d.seed_v = s->seed_v.p; d.seed_t = s->seed_t.p; d.nseed = s->nseed;
+  d.phi_init = s->warm;
   d.ctl = s->ctl.p;
   FimParams p{};
   p.dt = s->opts.dt;
@@ -897,4 +900,38 @@ extern "C" int fim_batch_get_stats(const fim_batch *b, fim_stats *out)
 {
   if (!b || !out) return batch_err(nullptr, FIM_ERR_INVALID_ARGUMENT, "fim_batch_get_stats: NULL argument");
   return fim_get_stats(b->s, out);
+}
+
+// ---------------------------------------------------------------------------
+// learned warm start: features of the staged problem, warm-start times
+
+extern "C" int fim_features(fim_solver *s, void *d_features, float *time_scale)
+{
+  if (!s || !d_features) return set_err(s, FIM_ERR_INVALID_ARGUMENT, "fim_features: NULL argument");
+  if (!s->have_mesh || !s->have_cond || !s->have_stim)
+    return set_err(s, FIM_ERR_NOT_READY, "fim_features: mesh, conduction and stimuli must be set first");
+  if (s->gptr.p) return set_err(s, FIM_ERR_INVALID_ARGUMENT, "fim_features: meshes with submesh tags are not supported");
+  CUDA_TRY(s, cudaSetDevice(s->device));
+  DevBuf<float> acc, dist;
+  DevBuf<unsigned int> red;
+  CUDA_TRY(s, acc.alloc(6 * (size_t)s->nV));
+  CUDA_TRY(s, dist.alloc((size_t)s->nV));
+  CUDA_TRY(s, red.alloc(8));
+  CUDA_TRY(s, launch_features((int)s->nV, s->nT, s->xyz.p, s->tslots.p, s->fib.p, s->cf.p, s->ct.p, s->nseed,
+                              s->seed_v.p, s->seed_t.p, acc.p, dist.p, red.p, d_features, s->stream));
+  unsigned int h[8] = {};
+  CUDA_TRY(s, cudaMemcpyAsync(h, red.p, sizeof(unsigned int) * 7, cudaMemcpyDeviceToHost, s->stream));
+  CUDA_TRY(s, cudaStreamSynchronize(s->stream));
+  if (time_scale) *time_scale = features_scale(h);
+  return FIM_OK;
+}
+
+extern "C" int fim_set_warm_start(fim_solver *s, const double *d_phi_init)
+{
+  if (!s) return set_err(nullptr, FIM_ERR_INVALID_ARGUMENT, "fim_set_warm_start: solver is NULL");
+  if (d_phi_init && (!s->have_mesh || s->gptr.p))
+    return set_err(s, FIM_ERR_INVALID_ARGUMENT, "fim_set_warm_start: needs a mesh without submesh tags");
+  s->warm = d_phi_init;
+  s->solved = false;
+  return FIM_OK;
 }

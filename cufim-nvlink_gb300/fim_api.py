@@ -26,7 +26,10 @@ EXPORTS = ["fim_default_opts", "fim_create", "fim_destroy", "fim_last_error", "f
            "fim_get_times", "fim_get_times_device", "fim_get_stats", "fim_vtk_read", "fim_vtk_write",
            "fim_read_tags", "fim_load_plan", "fim_set_stream", "fim_solve_noalloc", "fim_batch_create",
            "fim_batch_destroy", "fim_batch_last_error", "fim_batch_add", "fim_batch_solve", "fim_batch_get_times",
-           "fim_batch_get_stats"]
+           "fim_batch_get_stats", "fim_mlp_create", "fim_mlp_destroy", "fim_mlp_set_params", "fim_mlp_get_params",
+           "fim_mlp_gradients", "fim_mlp_train_step", "fim_mlp_predict", "fim_features", "fim_set_warm_start"]
+MLP_INPUTS = 64
+MLP_PARAMS = 41473
 
 
 class FimOpts(C.Structure):
@@ -88,6 +91,16 @@ def lib():
         L.fim_batch_solve.argtypes = [vp, vp]
         L.fim_batch_get_times.argtypes = [vp, i64, P(d), P(i32)]
         L.fim_batch_get_stats.argtypes = [vp, P(FimStats)]
+        f32 = C.c_float
+        L.fim_mlp_create.argtypes = [C.c_int, C.c_uint64, P(vp)]
+        L.fim_mlp_destroy.argtypes = [vp]
+        L.fim_mlp_set_params.argtypes = [vp, P(f32)]
+        L.fim_mlp_get_params.argtypes = [vp, P(f32)]
+        L.fim_mlp_gradients.argtypes = [vp, i64, vp, vp, P(f32), P(f32)]
+        L.fim_mlp_train_step.argtypes = [vp, i64, vp, vp, f32, P(f32)]
+        L.fim_mlp_predict.argtypes = [vp, i64, vp, vp]
+        L.fim_features.argtypes = [vp, vp, P(f32)]
+        L.fim_set_warm_start.argtypes = [vp, vp]
         L.fim_vtk_read.argtypes = [C.c_char_p, P(i64), P(i64), P(d), P(i64), P(i32)]
         L.fim_vtk_write.argtypes = [C.c_char_p, i64, i64, P(d), P(i64), P(i32), P(d), P(d)]
         L.fim_read_tags.argtypes = [C.c_char_p, P(i64), P(i32)]
@@ -195,6 +208,66 @@ class Solver:
         s = FimStats()
         _check(lib().fim_get_stats(self.h, C.byref(s)), self.h)
         return {k: getattr(s, k) for k, _ in FimStats._fields_}
+
+    def features(self, d_features):
+        """Writes the BF16 feature rows [n_vertices x MLP_INPUTS] to device memory; returns the time scale."""
+        ts = C.c_float()
+        _check(lib().fim_features(self.h, C.c_void_p(d_features), C.byref(ts)), self.h)
+        return ts.value
+
+    def set_warm_start(self, d_phi):
+        """Device address of FP64 start times [n_vertices] (kept alive by the caller), or None."""
+        _check(lib().fim_set_warm_start(self.h, C.c_void_p(d_phi) if d_phi else None), self.h)
+
+
+class Mlp:
+    """The warm-start network (a fim_mlp handle); device buffers are passed as addresses."""
+
+    def __init__(self, device=0, seed=1):
+        self.h = C.c_void_p()
+        _check(lib().fim_mlp_create(device, seed, C.byref(self.h)))
+
+    def close(self):
+        if self.h:
+            lib().fim_mlp_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def get_params(self):
+        p = np.empty(MLP_PARAMS, dtype=np.float32)
+        _check(lib().fim_mlp_get_params(self.h, _ptr(p, C.c_float)))
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        assert p.shape == (MLP_PARAMS,)
+        _check(lib().fim_mlp_set_params(self.h, _ptr(p, C.c_float)))
+
+    def gradients(self, n, d_features, d_targets):
+        g = np.empty(MLP_PARAMS, dtype=np.float32)
+        loss = C.c_float()
+        _check(lib().fim_mlp_gradients(self.h, n, C.c_void_p(d_features), C.c_void_p(d_targets), _ptr(g, C.c_float),
+                                       C.byref(loss)))
+        return g, loss.value
+
+    def train_step(self, n, d_features, d_targets, lr):
+        loss = C.c_float()
+        _check(lib().fim_mlp_train_step(self.h, n, C.c_void_p(d_features), C.c_void_p(d_targets), lr, C.byref(loss)))
+        return loss.value
+
+    def predict(self, n, d_features, d_out):
+        _check(lib().fim_mlp_predict(self.h, n, C.c_void_p(d_features), C.c_void_p(d_out)))
 
 
 def _bcheck(rc, b):

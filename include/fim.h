@@ -182,6 +182,46 @@ int fim_batch_get_times(fim_batch *b, int64_t problem, double *phi, int32_t *sta
 /* Statistics of the last batch solve (all problems together). */
 int fim_batch_get_stats(const fim_batch *b, fim_stats *out);
 
+/* Learned warm start -- no counterpart in the reference.
+ * A per-vertex MLP (features -> 128 -> 128 -> 128 -> 1, ReLU; BF16 weights
+ * on the tensor cores, FP32 accumulation, FP32 master weights and Adam)
+ * predicts activation times; fim_set_warm_start makes the next fim_solve
+ * start from given times (every vertex narrow at its start value, stimuli at
+ * their start times) and correct them downwards.  Such a solve is NOT
+ * bit-identical to the cold solve: the reference's FIM stops above the
+ * fixed point of its local solver, and that fixed point is not unique.
+ * Feature rows: FIM_MLP_INPUTS BF16 values per vertex, the first 7 used
+ * (x, y, z scaled to the bounding box; metric distance to the nearest
+ * stimulus over the time scale; cf; ct; fibre angle in the xy-plane / pi).
+ * Row counts passed to the network are multiples of 64 (pad with zeros). */
+#define FIM_MLP_INPUTS 64
+#define FIM_MLP_PARAMS 41473
+typedef struct fim_mlp fim_mlp;
+int fim_mlp_create(int device, uint64_t seed, fim_mlp **out);
+int fim_mlp_destroy(fim_mlp *m);
+/* Parameters (FIM_MLP_PARAMS floats: W1 [64x128], W2, W3 [128x128] row-major
+ * [in][out], then b1, b2, b3, w4, b4); setting them resets Adam. */
+int fim_mlp_set_params(fim_mlp *m, const float *params);
+int fim_mlp_get_params(const fim_mlp *m, float *params);
+/* Mean-squared-error gradients (host, FIM_MLP_PARAMS floats) and loss of n
+ * rows of d_features (device, BF16 [n x FIM_MLP_INPUTS]) against
+ * d_targets (device, FP32 [n]). */
+int fim_mlp_gradients(fim_mlp *m, int64_t n, const void *d_features, const float *d_targets, float *grads,
+                      float *loss);
+/* One Adam step on those n rows (learning rate lr); loss before the step. */
+int fim_mlp_train_step(fim_mlp *m, int64_t n, const void *d_features, const float *d_targets, float lr,
+                       float *loss);
+/* Predictions (device, FP32 [n]) for n feature rows. */
+int fim_mlp_predict(fim_mlp *m, int64_t n, const void *d_features, float *d_out);
+/* Feature rows (device, BF16 [n_vertices x FIM_MLP_INPUTS]) of the solver's
+ * mesh, conduction and stimuli (one submesh); *time_scale receives the
+ * largest stimulus distance, the unit of the distance feature and of the
+ * normalised times the network predicts. */
+int fim_features(fim_solver *s, void *d_features, float *time_scale);
+/* Start times (device, FP64 [n_vertices], kept by the caller until the
+ * solve) for the next solves; NULL restores the cold start. */
+int fim_set_warm_start(fim_solver *s, const double *d_phi_init);
+
 /* Reference-compatible files.  fim_vtk_* read/write the legacy ASCII VTK
  * that the reference reads and writes (load_vtk / save_vtk,
  * src/io/vtk.cpp:11-211); fim_read_tags reads a partition file

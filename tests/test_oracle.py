@@ -160,3 +160,30 @@ def test_planar_front_known_answer(O):
     seeds = np.nonzero(xyz[:, 0] == 0.0)[0]
     phi, _, _, _ = O.solve_pure(nV, slots, geo, seeds, np.zeros(len(seeds)))
     assert np.allclose(phi, xyz[:, 0] / 0.5, rtol=1e-6, atol=1e-9)
+
+
+def test_mlp_oracle_gradients_finite_differences():
+    """The network restatement's backward pass (FP64, no BF16 roundings)
+    against central finite differences of its loss."""
+    from oracle import mlp_oracle as M
+    rng = np.random.default_rng(4)
+    n = 32
+    p = np.zeros(M.NPARAMS)
+    p[M.OW1:M.OW1 + 7 * M.H] = rng.normal(0, 0.5, 7 * M.H)
+    p[M.OW2:M.OB1] = rng.normal(0, 0.12, 2 * M.H * M.H)
+    p[M.OB1:M.OW4] = rng.normal(0, 0.05, 3 * M.H)
+    p[M.OW4:M.OB4] = rng.normal(0, 0.1, M.H)
+    X = np.zeros((n, M.IN))
+    X[:, :7] = rng.normal(0, 1, (n, 7))
+    t = rng.normal(0, 1, n)
+    _, g = M.loss_and_gradients(p, X, t, exact=True)
+    idx = np.concatenate([rng.choice(np.arange(a, b), size=min(6, b - a), replace=False)
+                          for name, (a, b) in M.BLOCKS.items() if name != "W1"] +
+                         [rng.choice(np.arange(M.OW1, M.OW1 + 7 * M.H), size=6, replace=False)])
+    h = 1e-6
+    for i in idx:
+        pp, pm = p.copy(), p.copy()
+        pp[i] += h
+        pm[i] -= h
+        fd = (M.loss_and_gradients(pp, X, t, exact=True)[0] - M.loss_and_gradients(pm, X, t, exact=True)[0]) / (2 * h)
+        assert abs(fd - g[i]) <= 1e-6 + 1e-4 * abs(g[i]), (i, fd, g[i])
