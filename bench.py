@@ -38,8 +38,8 @@ import numpy as np  # noqa: E402
 SLAB_CELLS = (266, 93, 40)
 # DRAM bytes (read + write) of one fim_solve_kernel launch per vertex update,
 # from ncu dram__bytes_read.sum + dram__bytes_write.sum on this workload
-# (6.110 GB for 4,689,493 vertex updates; profiles/fim_solve_kernel_slab266x93x40_launches.md)
-NCU_DRAM_BYTES_PER_VERTEX_UPDATE = 6.110e9 / 4689493
+# (7.755 GB for 4,689,493 vertex updates; profiles/fim_solve_kernel_slab266x93x40_launches.md)
+NCU_DRAM_BYTES_PER_VERTEX_UPDATE = 7.755e9 / 4689493
 METRICS = {
     "slab": "slab solves/s (1.03M-vertex anisotropic FIM, bit-exact vs FP64 oracle)",
     "cube": "cube solves/s (9,261-vertex plain FIM, bit-exact vs FP64 oracle)",
