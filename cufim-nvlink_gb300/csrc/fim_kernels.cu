@@ -99,6 +99,47 @@ __device__ __forceinline__ double tet_ref(double e13, double e23, double e34, do
   return fmin(ra, rb);
 }
 
+// One of the two roots of tet_ref: second = false gives its "a" value
+// (pa + sqt X), true its "b" value (pa - sqt X, written as pa + (-(sqt X)),
+// which IEEE arithmetic rounds identically), so two lanes of a warp run one
+// instruction stream and tet_ref's result is the fmin of their values.
+__device__ __forceinline__ double tet_ref_root(double e13, double e23, double e34, double e12, double e14,
+                                               double e24, double p1, double p2, double p3, bool second)
+{
+  const double a = e13;
+  const double b = 0.5 * (e23 + e13 - e12);
+  const double c = -0.5 * (e34 + e13 - e14);
+  const double d = e23;
+  const double e = -0.5 * (e34 + e23 - e24);
+  const double f = e34;
+  const double q13 = p3 - p1;
+  const double q23 = p3 - p2;
+
+  const double sqt =
+    -e*e*c*d*d + a*d*d*d*d - (b*b*c - a*c*c)*f*f + ((b*b - a*c)*f*f -
+    (e*e*c - a*d*d - 2.*(e*c - b*d)*e)*f)*q13*q13 - 2.*(e*e*c*d -
+    2.*e*b*d*d + a*d*d*d + (b*b - a*c)*d*f)*q13*q23 + (e*e*c*c -
+    2.*e*b*c*d + a*c*d*d + (b*b*c - a*c*c)*f)*q23*q23 + 2.*(e*c*d*d -
+    b*d*d*d)*e + (e*e*c*c + (b*b - 2.*a*c)*d*d - 2.*(e*c*c - b*c*d)*e)*f;
+
+  if (sqt < 0.) return FIM_INF;
+
+  const double pa = e*c*d*d - b*d*d*d + (e*c - b*d)*f*q13*q13 - 2.*(e*c*d - b*d*d)*q13*q23 +
+                    (e*c*c - b*c*d)*q23*q23 - (e*c*c - b*c*d)*f;
+  const double pb = (d*d*d*d - 2.*c*d*d*f + c*c*f*f + (d*d*f - c*f*f)*q13*q13 -
+                     2.*(d*d*d - c*d*f)*q13*q23 + (c*d*d - c*c*f)*q23*q23);
+
+  const double sx = sqt*(d*q13 - c*q23);
+  const double l2 = (pa + (second ? -sx : sx))/pb;
+  const double l1 = -((f*l2 + e)*q13 - (d*l2 + b)*q23)/(d*q13 - c*q23);
+  const double l3 = 1 - l1 - l2;
+  double r = FIM_INF;
+  if ((l1 > 0. && l1 < 1.) && (l2 > 0. && l2 < 1.) && l3 > 0.)
+    r = l1*p1 + l2*p2 + l3*p3 + sqrt(a + 2.*l1*b + l1*l1*c + 2.*l1*l2*d + 2.*l2*e + l2*l2*f);
+  return r;
+}
+
+
 // ---------------------------------------------------------------------------
 // metric kernel
 
@@ -694,16 +735,44 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
     }
     __syncthreads();
 
-    // D: exact solves; tets from thread 0, triangles and edges each from the
-    // next warp boundary
+    // D: exact solves; tets (two lanes each) from thread 0, triangles and
+    // edges each from the next warp boundary
     {
       const int ntet = min(sh.nq[0], kQcap), ntri = min(sh.nq[1], kQcap), nedge = min(sh.nq[2], kQcap);
-      const int tri0 = (ntet + 31) & ~31;
+      // tets: two lanes each, one root per lane (tet_ref_root), warp-uniform loop
+      const int tri0 = (2 * ntet + 31) & ~31;
+      for (int jb = 0; jb < tri0; jb += kThreads) {
+        const int j = jb + tid;
+        double val = FIM_INF;
+        int slot = 0;
+        bool run = false;
+        if (j < 2 * ntet) {
+          const int pos = j >> 1;
+          const uint32_t it = sh.q[0][pos];
+          slot = it & 127;
+          run = !(sh.qlb[0][pos] > funkey(sh.bhi[slot]));  // else overtaken by a later bound
+          if (run) {
+            const int jj = (int)(it >> 9);
+            const int64_t c = sh.c0[slot] + (jj - sh.cp[slot]);
+            const int32_t *nb = sh.nb[jj];
+            const double p1 = __ldcg(d.phi + nb[0]), p2 = __ldcg(d.phi + nb[1]), p3 = __ldcg(d.phi + nb[2]);
+            const double2 *gp = reinterpret_cast<const double2 *>(d.cgeo + kCgeoStride * c);
+            const double2 t0 = __ldg(gp), t1 = __ldg(gp + 1), t2 = __ldg(gp + 2);
+            val = tet_ref_root(t0.x, t0.y, t1.x, t1.y, t2.x, t2.y, p1, p2, p3, (j & 1) != 0);
+          }
+        }
+        const double other = __shfl_xor_sync(FULL_MASK, val, 1);
+        if (run && !(j & 1)) {
+          const double v = fmin(val, other);
+          ++n_exact;
+          if (v < FIM_INF) atomicMin(&sh.res[slot], dkey(v));
+        }
+      }
       const int edge0 = tri0 + ((ntri + 31) & ~31);
-      for (int j = tid; j < edge0 + nedge; j += kThreads) {
+      for (int j = tid; j < edge0 + nedge; j += kThreads) {  // threads past the tets' warps: concurrently
         int qi, pos;
-        if (j < ntet) { qi = 0; pos = j; }
-        else if (j >= tri0 && j < tri0 + ntri) { qi = 1; pos = j - tri0; }
+        if (j < tri0) continue;
+        else if (j < tri0 + ntri) { qi = 1; pos = j - tri0; }
         else if (j >= edge0) { qi = 2; pos = j - edge0; }
         else continue;
         const uint32_t it = sh.q[qi][pos];
