@@ -44,15 +44,18 @@ __device__ __forceinline__ double tri_ref(double e12, double e13, double e23, do
   const double p12 = p2 - p1;
   float dv = (float)(p12 * p12 - c);
   const float sv = (float)((double)dv * (b * b - a * c));
-  if ((double)dv != 0.0 && (double)sv >= 0.0) {
+  // the reference compares the float intermediates after widening them to
+  // double; comparing the floats themselves gives the same answers (NaN too)
+  // without the FP64 conversions
+  if (dv != 0.f && sv >= 0.f) {
     dv = (float)(c * (double)dv);
     const float st = sqrtf(sv);
     const float l1 = (float)(-(b * p12 * p12 - b * c - (double)st * p12) / (double)dv);
     const float l2 = (float)(-(b * p12 * p12 - b * c + (double)st * p12) / (double)dv);
     float r1 = (float)(p2 - (double)l1 * p12 + sqrt(a + 2.0 * (double)l1 * b + (double)(l1 * l1) * c));
-    if (!(((double)l1 >= 0.0) && ((double)l1 <= 1.0))) r1 = (float)FIM_INF;
+    if (!((l1 >= 0.f) && (l1 <= 1.f))) r1 = (float)FIM_INF;
     float r2 = (float)(p2 - (double)l2 * p12 + sqrt(a + 2.0 * (double)l2 * b + (double)(l2 * l2) * c));
-    if (!(((double)l2 >= 0.0) && ((double)l2 <= 1.0))) r2 = (float)FIM_INF;
+    if (!((l2 >= 0.f) && (l2 <= 1.f))) r2 = (float)FIM_INF;
     return (double)fminf(r1, r2);
   }
   return FIM_INF;
