@@ -95,7 +95,7 @@ def workload(args):
                      "ct 0.24 mm/ms, 2 mm scar x0.1, 5 surface stimuli t0~U[0,10] ms; one submesh, "
                      "one endless window"),
         "vertices": nV, "tets": nT, "seed": 2,
-        "l2": "inputs larger than L2 (corner records 96 B x 4T)",
+        "l2": "inputs larger than L2 (corner records 128 B x 4T = 3.0 GB)",
         "parallelism": "replicas",
     }
     return case, cfg
