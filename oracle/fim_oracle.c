@@ -356,13 +356,17 @@ static void orc_sub_connect(orc_sub *S)
     for (int s = 0; s < 4; ++s) { const int32_t v = S->tv[4 * e + s]; S->n2e[fill[v]++] = e; }
   /* n2n: union of tet vertices, sorted unique */
   S->n2n_ptr = calloc(S->nn + 1, sizeof(int64_t));
-  int32_t *buf = malloc(sizeof(int32_t) * 4096);
+  /* gather buffer: four ids per incident tet of the busiest vertex */
+  int64_t maxdeg = 0;
+  for (int32_t v = 0; v < S->nn; ++v)
+    if (S->n2e_ptr[v + 1] - S->n2e_ptr[v] > maxdeg) maxdeg = S->n2e_ptr[v + 1] - S->n2e_ptr[v];
+  int32_t *buf = malloc(sizeof(int32_t) * (size_t)(4 * maxdeg + 1));
   int64_t cap = (int64_t)S->nn * 16 + 16, used = 0;
   S->n2n = malloc(sizeof(int32_t) * cap);
   for (int32_t v = 0; v < S->nn; ++v) {
     int nb = 0;
     for (int64_t k = S->n2e_ptr[v]; k < S->n2e_ptr[v + 1]; ++k)
-      for (int s = 0; s < 4; ++s) if (nb < 4096) buf[nb++] = S->tv[4 * S->n2e[k] + s];
+      for (int s = 0; s < 4; ++s) buf[nb++] = S->tv[4 * S->n2e[k] + s];
     qsort(buf, nb, sizeof(int32_t), cmp_i32);
     int m = 0;
     for (int i = 0; i < nb; ++i) if (m == 0 || buf[i] != buf[m - 1]) buf[m++] = buf[i];
@@ -597,36 +601,43 @@ static int orc_mesh_build(orc_mesh *M, int nV, int64_t nT, const int32_t *tv, co
   free(fill);
   M->n2n_ptr = calloc((size_t)nV + 1, sizeof(int64_t));
   int32_t *cnt = calloc((size_t)nV + 1, sizeof(int32_t));
+  /* gather buffer: four ids per incident tet of the busiest vertex */
+  int64_t maxdeg = 0;
+  for (int v = 0; v < nV; ++v)
+    if (M->n2e_ptr[v + 1] - M->n2e_ptr[v] > maxdeg) maxdeg = M->n2e_ptr[v + 1] - M->n2e_ptr[v];
+  const size_t bufn = (size_t)(4 * maxdeg + 1);
   /* two passes: count unique, then fill */
   #pragma omp parallel
   {
-    int32_t buf[2048];
+    int32_t *buf = malloc(sizeof(int32_t) * bufn);
     #pragma omp for schedule(static)
     for (int v = 0; v < nV; ++v) {
       int nb = 0;
       for (int64_t k = M->n2e_ptr[v]; k < M->n2e_ptr[v + 1]; ++k)
-        for (int s = 0; s < 4; ++s) if (nb < 2048) buf[nb++] = tv[4 * (int64_t)M->n2e[k] + s];
+        for (int s = 0; s < 4; ++s) buf[nb++] = tv[4 * (int64_t)M->n2e[k] + s];
       qsort(buf, nb, sizeof(int32_t), cmp_i32);
       int m = 0;
       for (int i = 0; i < nb; ++i) if (m == 0 || buf[i] != buf[m - 1]) buf[m++] = buf[i];
       cnt[v] = m;
     }
+    free(buf);
   }
   for (int v = 0; v < nV; ++v) M->n2n_ptr[v + 1] = M->n2n_ptr[v] + cnt[v];
   M->n2n = malloc(sizeof(int32_t) * (M->n2n_ptr[nV] + 1));
   #pragma omp parallel
   {
-    int32_t buf[2048];
+    int32_t *buf = malloc(sizeof(int32_t) * bufn);
     #pragma omp for schedule(static)
     for (int v = 0; v < nV; ++v) {
       int nb = 0;
       for (int64_t k = M->n2e_ptr[v]; k < M->n2e_ptr[v + 1]; ++k)
-        for (int s = 0; s < 4; ++s) if (nb < 2048) buf[nb++] = tv[4 * (int64_t)M->n2e[k] + s];
+        for (int s = 0; s < 4; ++s) buf[nb++] = tv[4 * (int64_t)M->n2e[k] + s];
       qsort(buf, nb, sizeof(int32_t), cmp_i32);
       int m = 0;
       for (int i = 0; i < nb; ++i) if (m == 0 || buf[i] != buf[m - 1]) buf[m++] = buf[i];
       memcpy(M->n2n + M->n2n_ptr[v], buf, sizeof(int32_t) * m);
     }
+    free(buf);
   }
   free(cnt);
   return 0;

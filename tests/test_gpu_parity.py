@@ -285,3 +285,35 @@ def test_shell_bit_exact(F, O):
     phi_o, st_o, it_o, _ = oracle_single(O, c)
     assert_identical(phi, st, phi_o, st_o)
     assert stats["iterations"] == it_o
+
+
+def _pincushion(n_sphere, seed):
+    """A centre vertex joined to every face of a triangulated sphere around
+    it: the centre has 2 n_sphere - 4 incident tets (more than one batch of
+    the solve kernel holds), the sphere vertices a handful each."""
+    from scipy.spatial import ConvexHull
+    rng = np.random.default_rng(seed)
+    p = rng.normal(size=(n_sphere, 3))
+    p /= np.linalg.norm(p, axis=1)[:, None]
+    hull = ConvexHull(p)
+    xyz = np.vstack([[[0.0, 0.0, 0.0]], p * rng.uniform(0.9, 1.1, (n_sphere, 1))])
+    tets = np.hstack([np.zeros((len(hull.simplices), 1), dtype=np.int64), hull.simplices + 1])
+    nT = tets.shape[0]
+    ang = rng.uniform(0, np.pi, nT)
+    fib = np.stack([np.cos(ang), np.sin(ang), np.zeros(nT)], axis=1)
+    return dict(xyz=xyz, tets=tets, fib=fib, cf=np.full(nT, 0.6), ct=np.full(nT, 0.25),
+                seed_v=np.array([1, 2, 3]), seed_t=np.array([0.0, 0.5, 1.0]))
+
+
+@pytest.mark.parametrize("n_sphere", [1400, 3000])
+def test_high_valence_vertex_bit_exact(F, O, n_sphere):
+    """A vertex with more corners than one batch holds (2,796 and 5,996
+    tets around it) goes through the all-FP64 path for the excess; the
+    result is still the oracle's, bit for bit, screened or not."""
+    pytest.importorskip("scipy")
+    c = _pincushion(n_sphere, 3)
+    phi_o, st_o, it_o, _ = oracle_single(O, c)
+    for exact_all in (0, 1):
+        phi, st, stats = F.solve_case(c, exact_all=exact_all)
+        assert_identical(phi, st, phi_o, st_o)
+        assert stats["iterations"] == it_o

@@ -187,3 +187,27 @@ def test_mlp_oracle_gradients_finite_differences():
         pm[i] -= h
         fd = (M.loss_and_gradients(pp, X, t, exact=True)[0] - M.loss_and_gradients(pm, X, t, exact=True)[0]) / (2 * h)
         assert abs(fd - g[i]) <= 1e-6 + 1e-4 * abs(g[i]), (i, fd, g[i])
+
+
+def test_high_valence_active_list_equals_reference_phases(O):
+    """The active-list oracle and the phase-by-phase restatement agree on a
+    vertex with thousands of incident tets (the neighbourhood lists of both
+    grow with the valence; no fixed-size gather)."""
+    pytest.importorskip("scipy")
+    from scipy.spatial import ConvexHull
+    rng = np.random.default_rng(3)
+    p = rng.normal(size=(3000, 3))
+    p /= np.linalg.norm(p, axis=1)[:, None]
+    hull = ConvexHull(p)
+    xyz = np.vstack([[[0.0, 0.0, 0.0]], p * rng.uniform(0.9, 1.1, (len(p), 1))])
+    tets = np.hstack([np.zeros((len(hull.simplices), 1), dtype=np.int64), hull.simplices + 1])
+    nT, nV = tets.shape[0], xyz.shape[0]
+    ang = rng.uniform(0, np.pi, nT)
+    fib = np.stack([np.cos(ang), np.sin(ang), np.zeros(nT)], axis=1)
+    slots, _, _, _ = O.reference_slots(nV, tets, None)
+    geo = O.metric_geo(slots, xyz, fib, np.full(nT, 0.6), np.full(nT, 0.25))
+    sv, st0 = np.array([1, 2, 3]), np.array([0.0, 0.5, 1.0])
+    phi, st, it, _ = O.solve_pure(nV, slots, geo, sv, st0)
+    fw = O.front_width(tets, xyz)
+    phi_r, st_r, it_r = O.solve_reference(nV, tets, None, geo, sv, st0, float("inf"), 1, fw, apd_us=-1.0)
+    assert np.array_equal(phi, phi_r) and np.array_equal(st, st_r) and it == it_r
