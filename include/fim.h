@@ -156,8 +156,8 @@ int fim_get_stats(const fim_solver *s, fim_stats *out);
 int fim_solve_noalloc(fim_solver *s, int64_t n, const int64_t *vertices, const double *t0,
                       double *d_phi, void *stream);
 
-/* Batched solves -- no counterpart in the reference (the benchmark spec's
- * batching: many solves of uneven size in one persistent launch).
+/* Batched solves -- no counterpart in the reference: many solves of uneven
+ * size in one persistent launch.
  * Independent problems (mesh + conduction + stimuli, each with its own
  * vertex numbering) are staged as one disjoint mesh and solved by ONE launch
  * of the persistent kernel: every FIM iteration advances all of them.  Each
