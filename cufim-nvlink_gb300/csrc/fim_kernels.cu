@@ -396,9 +396,16 @@ __device__ __forceinline__ double exact_solve(const FimDev &d, int64_t c, int ki
   const double2 *gp = reinterpret_cast<const double2 *>(d.cgeo + kCgeoStride * c);
   const double2 t0 = __ldg(gp), t1 = __ldg(gp + 1), t2 = __ldg(gp + 2);
   if (kind == 3) return tet_ref(t0.x, t0.y, t1.x, t1.y, t2.x, t2.y, p1, p2, p3);
-  if (kind == 0) return tri_ref(t1.y, t2.x, t2.y, p1, p2);
-  if (kind == 1) return tri_ref(t0.y, t2.y, t1.x, p2, p3);
-  return tri_ref(t0.x, t2.x, t1.x, p1, p3);
+  // the pair's operands are selected first, so that a warp whose lanes hold
+  // different pairs runs one triangle solve, not one per pair:
+  // (1,2): tri(e12, e14, e24, p1, p2); (2,3): tri(e23, e24, e34, p2, p3);
+  // (1,3): tri(e13, e14, e34, p1, p3)
+  const double e12 = kind == 0 ? t1.y : (kind == 1 ? t0.y : t0.x);
+  const double e13 = kind == 1 ? t2.y : t2.x;
+  const double e23 = kind == 0 ? t2.y : t1.x;
+  const double pa = kind == 1 ? p2 : p1;
+  const double pb = kind == 0 ? p2 : p3;
+  return tri_ref(e12, e13, e23, pa, pb);
 }
 
 // Position of e14, e24, e34 (the edges from neighbour 0, 1, 2 to the corner's
