@@ -142,6 +142,54 @@ __device__ __forceinline__ double tet_ref_root(double e13, double e23, double e3
   return r;
 }
 
+// The same tet solve with its long FP64 prefix (b, c, e, q13, q23, sqt, pa,
+// pb, sqt*X) spread over a group of kDagLanes lanes: the generated level
+// program (gen_tet_dag.py) gives each lane one DFMA per level on operands in
+// the group's scratch S, so the prefix costs kDagLevels dependent FP64
+// instructions instead of one per node.  The results are bit-identical to
+// tet_ref_root (every node is one correctly rounded operation of the source's
+// own expression tree).
+#include "tet_dag.inc"
+
+__device__ __forceinline__ double flip_sign(double x, uint32_t flip)
+{
+  return __longlong_as_double(__double_as_longlong(x) ^ ((unsigned long long)(flip != 0u) << 63));
+}
+
+// Runs the level program on scratch S (leaves already stored); gl is the
+// lane's index in its group.  All lanes of the warp take part.
+__device__ __forceinline__ void tet_dag_prefix(double *S, int gl)
+{
+#pragma unroll
+  for (int lv = 0; lv < kDagLevels; ++lv) {
+    const uint32_t w = kTetDagProg[lv][gl];
+    const double A = flip_sign(S[w & 255u], w & (1u << 24));
+    const double B = flip_sign(S[(w >> 8) & 255u], w & (1u << 25));
+    const double C = flip_sign(S[(w >> 16) & 255u], w & (1u << 26));
+    S[kDagLeaves + lv * kDagLanes + gl] = fma(A, B, C);
+    __syncwarp();
+  }
+}
+
+// The root part of tet_ref_root on the prefix in S (second: its "b" root).
+__device__ __forceinline__ double tet_root_tail(const double *S, bool second)
+{
+  const double a = S[kDagLeafE13], d = S[kDagLeafE13 + 1], f = S[kDagLeafE13 + 2];
+  const double b = S[kDagOut_b], c = S[kDagOut_c], e = S[kDagOut_e];
+  const double p1 = S[kDagLeafP1], p2 = S[kDagLeafP1 + 1], p3 = S[kDagLeafP1 + 2];
+  const double q13 = S[kDagOut_q13], q23 = S[kDagOut_q23];
+  const double sqt = S[kDagOut_sqt];
+  if (sqt < 0.) return FIM_INF;
+  const double pa = S[kDagOut_pa], pb = S[kDagOut_pb], sx = S[kDagOut_sx], X = S[kDagOut_X];
+  const double l2 = (pa + (second ? -sx : sx))/pb;
+  const double l1 = -((f*l2 + e)*q13 - (d*l2 + b)*q23)/X;
+  const double l3 = 1 - l1 - l2;
+  double r = FIM_INF;
+  if ((l1 > 0. && l1 < 1.) && (l2 > 0. && l2 < 1.) && l3 > 0.)
+    r = l1*p1 + l2*p2 + l3*p3 + sqrt(a + 2.*l1*b + l1*l1*c + 2.*l1*l2*d + 2.*l2*e + l2*l2*f);
+  return r;
+}
+
 
 // ---------------------------------------------------------------------------
 // metric kernel
@@ -329,6 +377,10 @@ constexpr int kCornerCap = 2560;    // corners per batch
 constexpr int kTriCap = kCornerCap * 3 / 2;  // triangle screens per batch (more are screened on the spot)
 constexpr int kTetCap = kCornerCap; // tet screens per batch: never full
 constexpr int kQcap = 1024;         // exact solves queued per kind and batch
+// Phase D runs the queued tets on at most kDagWarps warps, one group of
+// kDagLanes lanes per tet (scratch: kDagGroups * kDagSlots doubles).
+constexpr int kDagWarps = 7;
+constexpr int kDagGroups = kDagWarps * 32 / kDagLanes;
 
 // Order-preserving map of floats to unsigned integers (for atomicMin).
 __device__ __forceinline__ unsigned int fkey(float x)
@@ -357,7 +409,10 @@ struct BatchSh {
   int32_t nb[kCornerCap][3];        // the other three vertices
   float pf[kCornerCap][3];          // their float times
   float sf[kCornerCap][3];          // float edge lengths sqrt(e14), sqrt(e24), sqrt(e34)
-  float lbt[kCornerCap][4];         // root-term bounds, then lower bounds of pairs (1,2), (2,3), (1,3) and tet
+  union {
+    float lbt[kCornerCap][4];       // root-term bounds, then lower bounds of pairs (1,2), (2,3), (1,3) and tet
+    double dag[kDagGroups][kDagSlots];  // phase D: scratch of the tet prefix groups
+  };
   uint8_t vm[kCornerCap];           // validity bits of the three neighbours
   uint8_t cs[kCornerCap];           // slot of the corner's vertex
   // compacted screen lists: item (corner j | pair k << 16)
@@ -366,8 +421,12 @@ struct BatchSh {
   uint32_t q[3][kQcap];             // queued exact solves: [0] tets, [1] triangles, [2] edges
   float qlb[3][kQcap];              // their lower bounds (rechecked against the final bhi)
   int ntri, ntet, nq[3];
+  int next_item;                    // next unclaimed screen item (phase S)
   int nslot;                        // vertices of the current batch
 };
+
+static_assert(sizeof(double) * kDagGroups * kDagSlots <= sizeof(float) * kCornerCap * 4,
+              "the tet prefix scratch must fit in the lower-bound array it overlays");
 
 // Queue item: slot (7 bits) | kind (2 bits) | corner index in the batch (23 bits).
 // kind: triangle pair 0..2 or 3 (tet) in queues 0 and 1, edge 0..2 in queue 2.
@@ -405,6 +464,19 @@ __device__ __forceinline__ double exact_solve(const FimDev &d, int64_t c, int ki
   const double e23 = kind == 0 ? t2.y : t1.x;
   const double pa = kind == 1 ? p2 : p1;
   const double pb = kind == 0 ? p2 : p3;
+  return tri_ref(e12, e13, e23, pa, pb);
+}
+
+// FP64 triangle solve kind 0..2 of corner c (exact_solve without its tet
+// branch, for the warps that run only triangle solves).
+__device__ __forceinline__ double exact_tri(const FimDev &d, int64_t c, int kind, const int32_t *nb)
+{
+  const double pa = __ldcg(d.phi + nb[kind == 1 ? 1 : 0]), pb = __ldcg(d.phi + nb[kind == 0 ? 1 : 2]);
+  const double2 *gp = reinterpret_cast<const double2 *>(d.cgeo + kCgeoStride * c);
+  const double2 t0 = __ldg(gp), t1 = __ldg(gp + 1), t2 = __ldg(gp + 2);
+  const double e12 = kind == 0 ? t1.y : (kind == 1 ? t0.y : t0.x);
+  const double e13 = kind == 1 ? t2.y : t2.x;
+  const double e23 = kind == 0 ? t2.y : t1.x;
   return tri_ref(e12, e13, e23, pa, pb);
 }
 
@@ -530,7 +602,7 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
     }
     if (tid == 0) {
       sh.cp[0] = 0;
-      sh.ntri = 0; sh.ntet = 0; sh.nq[0] = 0; sh.nq[1] = 0; sh.nq[2] = 0;
+      sh.ntri = 0; sh.ntet = 0; sh.nq[0] = 0; sh.nq[1] = 0; sh.nq[2] = 0; sh.next_item = 0;
     }
     __syncthreads();
     if (tid < 32) {
@@ -701,16 +773,21 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
     }
     __syncthreads();
 
-    // S: screens over the compacted lists (tets from thread 0, triangles from
-    // the next warp boundary, so that every warp holds one kind); a solve
-    // whose lower bound does not exceed the current bhi is queued at once
-    // (bhi only decreases: phase D rechecks against the final bound)
+    // S: screens over the compacted lists, handed out in chunks of 32 items
+    // (one per lane) to whichever warp is free -- tets first, then triangles
+    // from the next chunk boundary, so that every chunk holds one kind; a
+    // solve whose lower bound does not exceed the current bhi is queued at
+    // once (bhi only decreases: phase D rechecks against the final bound)
     {
       const int ntet = min(sh.ntet, kTetCap), ntri = min(sh.ntri, kTriCap);
       const int tri0 = (ntet + 31) & ~31;
-      for (int ib = 0; ib < tri0 + ntri; ib += kThreads) {
-        const int i = ib + tid;
-        const int qi = ib + (tid & ~31) < tri0 ? 0 : 1;  // the same on every lane of the warp
+      for (;;) {
+        int ib = 0;
+        if (lane == 0) ib = atomicAdd(&sh.next_item, 32);
+        ib = __shfl_sync(FULL_MASK, ib, 0);
+        if (ib >= tri0 + ntri) break;
+        const int i = ib + lane;
+        const int qi = ib < tri0 ? 0 : 1;  // the same on every lane of the warp
         bool need = false;
         int kind = 0, slot = 0, j = 0;
         float lb = 0.f;
@@ -745,37 +822,46 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
     }
     __syncthreads();
 
-    // D: exact solves; tets (two lanes each) from thread 0, triangles and
+    // D: exact solves; tets (a lane group each) from thread 0, triangles and
     // edges each from the next warp boundary
     {
       const int ntet = min(sh.nq[0], kQcap), ntri = min(sh.nq[1], kQcap), nedge = min(sh.nq[2], kQcap);
-      // tets: two lanes each, one root per lane (tet_ref_root), warp-uniform loop
-      const int tri0 = (2 * ntet + 31) & ~31;
-      for (int jb = 0; jb < tri0; jb += kThreads) {
-        const int j = jb + tid;
-        double val = FIM_INF;
-        int slot = 0;
-        bool run = false;
-        if (j < 2 * ntet) {
-          const int pos = j >> 1;
-          const uint32_t it = sh.q[0][pos];
-          slot = it & 127;
-          run = !(sh.qlb[0][pos] > funkey(sh.bhi[slot]));  // else overtaken by a later bound
-          if (run) {
-            const int jj = (int)(it >> 9);
-            const int64_t c = sh.c0[slot] + (jj - sh.cp[slot]);
-            const int32_t *nb = sh.nb[jj];
-            const double p1 = __ldcg(d.phi + nb[0]), p2 = __ldcg(d.phi + nb[1]), p3 = __ldcg(d.phi + nb[2]);
-            const double2 *gp = reinterpret_cast<const double2 *>(d.cgeo + kCgeoStride * c);
-            const double2 t0 = __ldg(gp), t1 = __ldg(gp + 1), t2 = __ldg(gp + 2);
-            val = tet_ref_root(t0.x, t0.y, t1.x, t1.y, t2.x, t2.y, p1, p2, p3, (j & 1) != 0);
+      // tets: one group of kDagLanes lanes per tet runs the prefix
+      // (tet_dag_prefix), then the group's first two lanes one root each;
+      // groups of kDagWarps warps at most, warp-uniform loop
+      const int tet_warps = min(kDagWarps, (ntet * kDagLanes + 31) / 32);
+      const int tri0 = 32 * tet_warps;
+      if (tid < tri0) {
+        const int grp = tid / kDagLanes, gl = tid % kDagLanes;
+        double *S = sh.dag[grp];
+        for (int base = 0; base < ntet; base += tri0 / kDagLanes) {
+          const int pos = base + grp;
+          int slot = 0;
+          bool run = false;
+          if (pos < ntet) {
+            const uint32_t it = sh.q[0][pos];
+            slot = it & 127;
+            run = !(sh.qlb[0][pos] > funkey(sh.bhi[slot]));  // else overtaken by a later bound
+            if (run) {
+              const int jj = (int)(it >> 9);
+              const int64_t c = sh.c0[slot] + (jj - sh.cp[slot]);
+              // leaves: e13 e23 e34 e12 e14 e24 p1 p2 (lanes 0..7), p3, 0.5 2.0 1.0 -0.0
+              S[gl] = gl < 6 ? __ldg(d.cgeo + kCgeoStride * c + gl) : __ldcg(d.phi + sh.nb[jj][gl - 6]);
+              if (gl == 0) S[kDagLeafP1 + 2] = __ldcg(d.phi + sh.nb[jj][2]);
+              else if (gl <= 4) S[kDagLeafConst + gl - 1] = gl == 1 ? 0.5 : (gl == 2 ? 2.0 : (gl == 3 ? 1.0 : -0.0));
+            }
           }
-        }
-        const double other = __shfl_xor_sync(FULL_MASK, val, 1);
-        if (run && !(j & 1)) {
-          const double v = fmin(val, other);
-          ++n_exact;
-          if (v < FIM_INF) atomicMin(&sh.res[slot], dkey(v));
+          __syncwarp();
+          tet_dag_prefix(S, gl);
+          double val = FIM_INF;
+          if (run && gl < 2) val = tet_root_tail(S, gl == 1);
+          const double other = __shfl_xor_sync(FULL_MASK, val, 1);
+          if (run && gl == 0) {
+            const double v = fmin(val, other);
+            ++n_exact;
+            if (v < FIM_INF) atomicMin(&sh.res[slot], dkey(v));
+          }
+          __syncwarp();  // the next pass overwrites S
         }
       }
       const int edge0 = tri0 + ((ntri + 31) & ~31);
@@ -787,7 +873,10 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
         else continue;
         const uint32_t it = sh.q[qi][pos];
         if (sh.qlb[qi][pos] > funkey(sh.bhi[it & 127])) continue;  // overtaken by a later bound
-        run_item(d, sh, qi, it);
+        const int slot = it & 127, kind = (it >> 7) & 3, jj = (int)(it >> 9);
+        const int64_t c = sh.c0[slot] + (jj - sh.cp[slot]);
+        const double val = qi == 2 ? exact_edge(d, c, kind, sh.nb[jj][kind]) : exact_tri(d, c, kind, sh.nb[jj]);
+        if (val < FIM_INF) atomicMin(&sh.res[slot], dkey(val));
         if (qi < 2) ++n_exact;
       }
     }
