@@ -14,8 +14,16 @@ enum : uint8_t { ST_FAR = 0, ST_NEIG = 1, ST_NARROW = 2, ST_NEXT = 3, ST_FROZEN 
 
 // Doubles per corner of the FP64 record.
 constexpr int kCgeoStride = 6;
-// Floats per corner of the FP32 screen record.
-constexpr int kCgfStride = 16;
+// Floats per corner of the FP32 screen record (e13, e23, e34, e12, e14, e24
+// times 2^-k, k, unused).
+constexpr int kCgfStride = 8;
+// The 32-byte record that every corner update reads first, as two uint4:
+//   [0] ids of the other three vertices ("1","2","3"), root-term bounds of
+//       the pairs (1,2) and (2,3) as two fp16 rounded down;
+//   [1] float edge lengths towards the corner's vertex from "1","2","3",
+//       root-term bounds of the pair (1,3) and of the tet as two fp16.
+// The ids come from the mesh staging, the rest from the metric kernel.
+constexpr int kCrecWords = 2;
 
 // Threads per block of the persistent solve kernel (one block per SM).
 constexpr int kSolveThreads = 512;
@@ -58,10 +66,9 @@ struct FimDev {
   int64_t nC;                 // corners = 4 * nT
   // topology
   const int64_t *cptr;        // [nV+1] corner range per vertex
-  const int4 *cids;           // [nC] other three vertices of the corner ("1","2","3"), w unused
+  const uint4 *crec;          // [kCrecWords*nC] first-read record of each corner (kCrecWords)
   const double *cgeo;         // [nC*kCgeoStride] FP64 e13, e23, e34, e12, e14, e24
-  const float *cgf;           // [nC*kCgfStride] float screen record: e13..e24 * 2^-k, sqrt(e14,e24,e34), k, bad,
-                              //   pad, root-term bounds of pairs (1,2), (2,3), (1,3) and of the tet
+  const float *cgf;           // [nC*kCgfStride] float screen record: e13..e24 * 2^-k, k, unused
   float *phi_f;               // float copy (round to nearest) of phi, kept in step with it
   const int64_t *nptr;        // [nV+1] vertex neighbourhood (self included)
   const int32_t *nbr;
@@ -101,7 +108,7 @@ void set_last_error(const char *msg);
 // FP64 metric + edge norms per tet scattered into the corner records.
 cudaError_t launch_metric(const int32_t *tslots, const int64_t *cidx, const double *xyz,
                           const double *fib, const double *cf, const double *ct, int64_t nT,
-                          double *cgeo, float *cgf, cudaStream_t stream);
+                          double *cgeo, float *cgf, uint4 *crec, cudaStream_t stream);
 // Persistent cooperative solve.
 cudaError_t launch_solve(const FimDev &d, const FimParams &p, int grid, int block, cudaStream_t stream);
 // Occupancy-derived grid size for the cooperative launch.

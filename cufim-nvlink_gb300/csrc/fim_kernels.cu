@@ -26,6 +26,7 @@
 
 #include <cfloat>
 #include <cstdint>
+#include <cuda_fp16.h>
 
 namespace fimgb {
 
@@ -214,10 +215,20 @@ __host__ __device__ constexpr int sel_of(int t, int k)
        :          edge_index((t + 2) & 3, t);
 }
 
+// Two non-negative lower bounds as fp16 rounded towards -inf (so they stay
+// lower bounds), packed low | high << 16.
+__device__ __forceinline__ uint32_t half_pair_rd(float lo, float hi)
+{
+  return (uint32_t)__half_as_ushort(__float2half_rd(lo)) | ((uint32_t)__half_as_ushort(__float2half_rd(hi)) << 16);
+}
+__device__ __forceinline__ float half_lo(uint32_t w) { return __half2float(__ushort_as_half((unsigned short)(w & 0xffffu))); }
+__device__ __forceinline__ float half_hi(uint32_t w) { return __half2float(__ushort_as_half((unsigned short)(w >> 16))); }
+
 __global__ void fim_metric_kernel(const int32_t *__restrict__ tslots, const int64_t *__restrict__ cidx,
                                   const double *__restrict__ xyz, const double *__restrict__ fib,
                                   const double *__restrict__ cf, const double *__restrict__ ct,
-                                  int64_t nT, double *__restrict__ cgeo, float *__restrict__ cgf)
+                                  int64_t nT, double *__restrict__ cgeo, float *__restrict__ cgf,
+                                  uint4 *__restrict__ crec)
 {
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nT;
        e += (int64_t)gridDim.x * blockDim.x) {
@@ -278,9 +289,13 @@ __global__ void fim_metric_kernel(const int32_t *__restrict__ tslots, const int6
       corner_bounds(gs, ok ? ks : 0, hb);
       if (!ok) hb[0] = hb[1] = hb[2] = hb[3] = 0.f;
       of[0] = make_float4(gs[0], gs[1], gs[2], gs[3]);
-      of[1] = make_float4(gs[4], gs[5], len[sel_of(t, 4)], len[sel_of(t, 5)]);
-      of[2] = make_float4(len[sel_of(t, 2)], (float)ks, ok ? 0.f : 1.f, 0.f);
-      of[3] = make_float4(hb[0], hb[1], hb[2], hb[3]);
+      of[1] = make_float4(gs[4], gs[5], (float)ks, 0.f);
+      // first-read record: the lengths and the bounds (fp16, rounded down, so
+      // still lower bounds); its ids were written at mesh staging
+      uint4 *rc = crec + kCrecWords * c;
+      rc[0].w = half_pair_rd(hb[0], hb[1]);
+      rc[1] = make_uint4(__float_as_uint(len[sel_of(t, 4)]), __float_as_uint(len[sel_of(t, 5)]),
+                         __float_as_uint(len[sel_of(t, 2)]), half_pair_rd(hb[2], hb[3]));
     }
   }
 }
@@ -518,8 +533,8 @@ __device__ __forceinline__ void screen_record(const FimDev &d, const BatchSh &sh
 {
   const int slot = sh.cs[j];
   const float4 *rp = reinterpret_cast<const float4 *>(d.cgf + kCgfStride * (sh.c0[slot] + (j - sh.cp[slot])));
-  const float4 r0 = __ldg(rp), r1 = __ldg(rp + 1), r2 = __ldg(rp + 2);
-  g[0] = r0.x; g[1] = r0.y; g[2] = r0.z; g[3] = r0.w; g[4] = r1.x; g[5] = r1.y; g[6] = r2.y;
+  const float4 r0 = __ldg(rp), r1 = __ldg(rp + 1);
+  g[0] = r0.x; g[1] = r0.y; g[2] = r0.z; g[3] = r0.w; g[4] = r1.x; g[5] = r1.y; g[6] = r1.z;
 }
 
 // FP32 screens of triangle pair k (0: (1,2), 1: (2,3), 2: (1,3)) and of the
@@ -635,11 +650,17 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
     // the neighbours' states and float times; within a pass the loads of a
     // thread's corners are independent, so they are all in flight together.
     for (int jb = 0; jb < kept; jb += kPer * kThreads) {
+      // all of a thread's record loads first, then the neighbour loads that
+      // need their ids, then the stores: every load of a pass is in flight
+      // at once
       int slot[kPer];
+      uint4 h0[kPer], h1[kPer];
 #pragma unroll
       for (int r = 0; r < kPer; ++r) {
         const int j = jb + tid + r * kThreads;
         slot[r] = 0;
+        h0[r] = make_uint4(0u, 0u, 0u, 0u);
+        h1[r] = h0[r];
         if (j < kept) {
           int lo = 0, hi = nslot - 1;  // last slot with cp[slot] <= j
           while (lo < hi) {
@@ -648,13 +669,8 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
           }
           slot[r] = lo;
           const int64_t c = sh.c0[lo] + (j - sh.cp[lo]);
-          const int4 id = __ldg(d.cids + c);
-          const float4 *rp = reinterpret_cast<const float4 *>(d.cgf + kCgfStride * c);
-          const float4 r1 = __ldg(rp + 1), r2 = __ldg(rp + 2), r3 = __ldg(rp + 3);
-          sh.lbt[j][0] = r3.x; sh.lbt[j][1] = r3.y; sh.lbt[j][2] = r3.z; sh.lbt[j][3] = r3.w;
-          sh.nb[j][0] = id.x; sh.nb[j][1] = id.y; sh.nb[j][2] = id.z;
-          sh.sf[j][0] = r1.z; sh.sf[j][1] = r1.w; sh.sf[j][2] = r2.x;
-          sh.cs[j] = (uint8_t)lo;
+          h0[r] = __ldg(d.crec + kCrecWords * c);
+          h1[r] = __ldg(d.crec + kCrecWords * c + 1);
         }
       }
       float pf[kPer][3];
@@ -663,12 +679,24 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
       for (int r = 0; r < kPer; ++r) {
         const int j = jb + tid + r * kThreads;
         if (j < kept) {
+          const int32_t nbs[3] = {(int32_t)h0[r].x, (int32_t)h0[r].y, (int32_t)h0[r].z};
 #pragma unroll
           for (int i = 0; i < 3; ++i) {
-            const int32_t nbi = sh.nb[j][i];
-            pf[r][i] = __ldcg(d.phi_f + nbi);
-            stn[r][i] = __ldcg(d.st + nbi);
+            pf[r][i] = __ldcg(d.phi_f + nbs[i]);
+            stn[r][i] = __ldcg(d.st + nbs[i]);
           }
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < kPer; ++r) {
+        const int j = jb + tid + r * kThreads;
+        if (j < kept) {
+          sh.lbt[j][0] = half_lo(h0[r].w); sh.lbt[j][1] = half_hi(h0[r].w);
+          sh.lbt[j][2] = half_lo(h1[r].w); sh.lbt[j][3] = half_hi(h1[r].w);
+          sh.nb[j][0] = (int32_t)h0[r].x; sh.nb[j][1] = (int32_t)h0[r].y; sh.nb[j][2] = (int32_t)h0[r].z;
+          sh.sf[j][0] = __uint_as_float(h1[r].x); sh.sf[j][1] = __uint_as_float(h1[r].y);
+          sh.sf[j][2] = __uint_as_float(h1[r].z);
+          sh.cs[j] = (uint8_t)slot[r];
         }
       }
 #pragma unroll
@@ -714,8 +742,8 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
     for (int j = kept + tid; j < total; j += kThreads) {
       const int slot = 0;  // only a batch of one vertex has such corners
       const int64_t c = sh.c0[slot] + (j - sh.cp[slot]);
-      const int4 id = __ldg(d.cids + c);
-      const int32_t nb[3] = {id.x, id.y, id.z};
+      const uint4 id = __ldg(d.crec + kCrecWords * c);
+      const int32_t nb[3] = {(int32_t)id.x, (int32_t)id.y, (int32_t)id.z};
       uint32_t m = 0;
       for (int i = 0; i < 3; ++i) {
         const double p = __ldcg(d.phi + nb[i]);
@@ -1096,13 +1124,13 @@ __global__ void __launch_bounds__(kThreads, 1) fim_solve_kernel(FimDev d, FimPar
 
 cudaError_t launch_metric(const int32_t *tslots, const int64_t *cidx, const double *xyz,
                           const double *fib, const double *cf, const double *ct, int64_t nT,
-                          double *cgeo, float *cgf, cudaStream_t stream)
+                          double *cgeo, float *cgf, uint4 *crec, cudaStream_t stream)
 {
   if (nT <= 0) return cudaSuccess;
   const int block = 256;
   int64_t grid = (nT + block - 1) / block;
   if (grid > 152 * 64) grid = 152 * 64;
-  fim_metric_kernel<<<(unsigned)grid, block, 0, stream>>>(tslots, cidx, xyz, fib, cf, ct, nT, cgeo, cgf);
+  fim_metric_kernel<<<(unsigned)grid, block, 0, stream>>>(tslots, cidx, xyz, fib, cf, ct, nT, cgeo, cgf, crec);
   return cudaGetLastError();
 }
 

@@ -91,7 +91,7 @@ struct fim_solver {
   DevBuf<double> xyz;
   DevBuf<int32_t> tslots;
   DevBuf<int64_t> cidx, cptr, nptr;
-  DevBuf<int4> cids;
+  DevBuf<uint4> crec;
   DevBuf<double> cgeo;
   DevBuf<float> cgf, phi_f;
   DevBuf<int32_t> nbr;
@@ -410,7 +410,7 @@ extern "C" int fim_set_mesh(fim_solver *s, int64_t nV, const double *xyz, int64_
   CUDA_TRY(s, s->tslots.alloc(4 * nT));
   CUDA_TRY(s, s->cidx.alloc(nC));
   CUDA_TRY(s, s->cptr.alloc(nL + 1));
-  CUDA_TRY(s, s->cids.alloc(nC));
+  CUDA_TRY(s, s->crec.alloc((size_t)kCrecWords * nC));
   CUDA_TRY(s, s->cgeo.alloc((size_t)kCgeoStride * nC));
   CUDA_TRY(s, s->cgf.alloc((size_t)kCgfStride * nC));
   CUDA_TRY(s, s->nptr.alloc(nL + 1));
@@ -443,7 +443,17 @@ extern "C" int fim_set_mesh(fim_solver *s, int64_t nV, const double *xyz, int64_
   CUDA_TRY(s, cudaMemcpyAsync(s->tslots.p, slots.data(), sizeof(int32_t) * 4 * nT, cudaMemcpyHostToDevice, st));
   CUDA_TRY(s, cudaMemcpyAsync(s->cidx.p, cidx.data(), sizeof(int64_t) * nC, cudaMemcpyHostToDevice, st));
   CUDA_TRY(s, cudaMemcpyAsync(s->cptr.p, cptr.data(), sizeof(int64_t) * (nL + 1), cudaMemcpyHostToDevice, st));
-  CUDA_TRY(s, cudaMemcpyAsync(s->cids.p, cids.data(), sizeof(int4) * nC, cudaMemcpyHostToDevice, st));
+  {
+    // the ids part of the first-read records (the metric kernel fills the rest)
+    std::vector<uint4> crec((size_t)kCrecWords * nC);
+#pragma omp parallel for schedule(static)
+    for (int64_t c = 0; c < nC; ++c) {
+      crec[kCrecWords * c] = make_uint4((unsigned)cids[c].x, (unsigned)cids[c].y, (unsigned)cids[c].z, 0u);
+      crec[kCrecWords * c + 1] = make_uint4(0u, 0u, 0u, 0u);
+    }
+    CUDA_TRY(s, cudaMemcpyAsync(s->crec.p, crec.data(), sizeof(uint4) * crec.size(), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(s, cudaStreamSynchronize(st));
+  }
   CUDA_TRY(s, cudaMemcpyAsync(s->nptr.p, nptr.data(), sizeof(int64_t) * (nL + 1), cudaMemcpyHostToDevice, st));
   CUDA_TRY(s, cudaMemcpyAsync(s->nbr.p, nbr.data(), sizeof(int32_t) * nbr.size(), cudaMemcpyHostToDevice, st));
   if (multi) {
@@ -460,7 +470,7 @@ static int run_metric(fim_solver *s)
 {
   CUDA_TRY(s, cudaEventRecord(s->ev0, s->stream));
   CUDA_TRY(s, launch_metric(s->tslots.p, s->cidx.p, s->xyz.p, s->fib.p, s->cf.p, s->ct.p, s->nT, s->cgeo.p, s->cgf.p,
-                            s->stream));
+                            s->crec.p, s->stream));
   CUDA_TRY(s, cudaEventRecord(s->ev1, s->stream));
   CUDA_TRY(s, cudaEventSynchronize(s->ev1));
   float ms = 0.f;
@@ -570,7 +580,7 @@ extern "C" int fim_solve(fim_solver *s, void *stream)
   FimDev d{};
   d.nV = (int32_t)s->nL; d.nG = (int32_t)s->nV; d.nT = s->nT; d.nC = s->nC;
   d.gptr = s->gptr.p; d.gcopy = s->gcopy.p; d.phi_out = s->phi_out.p; d.st_out = s->st_out.p;
-  d.cptr = s->cptr.p; d.cids = s->cids.p; d.cgeo = s->cgeo.p; d.cgf = s->cgf.p; d.nptr = s->nptr.p; d.nbr = s->nbr.p;
+  d.cptr = s->cptr.p; d.crec = s->crec.p; d.cgeo = s->cgeo.p; d.cgf = s->cgf.p; d.nptr = s->nptr.p; d.nbr = s->nbr.p;
   d.phi_f = s->phi_f.p;
   d.phi = s->phi.p; d.phi2 = s->phi2.p; d.st = s->st.p; d.tst = s->tst.p; d.flag = s->flag.p;
   d.list[0] = s->list0.p; d.list[1] = s->list1.p; d.list[2] = s->list2.p;
@@ -708,7 +718,7 @@ extern "C" int fim_solve_noalloc(fim_solver *s, int64_t n, const int64_t *vertic
   d.nV = (int32_t)s->nL; d.nG = (int32_t)s->nV; d.nT = s->nT; d.nC = s->nC;
   d.gptr = s->gptr.p; d.gcopy = s->gcopy.p;
   d.phi_out = multi ? d_phi : nullptr; d.st_out = multi ? sc.st_out : nullptr;
-  d.cptr = s->cptr.p; d.cids = s->cids.p; d.cgeo = s->cgeo.p; d.cgf = s->cgf.p; d.nptr = s->nptr.p; d.nbr = s->nbr.p;
+  d.cptr = s->cptr.p; d.crec = s->crec.p; d.cgeo = s->cgeo.p; d.cgf = s->cgf.p; d.nptr = s->nptr.p; d.nbr = s->nbr.p;
   d.phi_f = sc.phi_f;
   d.phi = sc.phi; d.phi2 = sc.phi2; d.st = sc.st; d.tst = sc.tst; d.flag = sc.flag;
   d.list[0] = sc.list[0]; d.list[1] = sc.list[1]; d.list[2] = sc.list[2];
