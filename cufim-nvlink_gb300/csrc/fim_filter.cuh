@@ -112,7 +112,7 @@ __device__ __forceinline__ CandBound tri_screen(Re e12, Re e13, Re e23, Re p1, R
   const Re BPC = (B * P12) * P12 - B * C;
   const Re SP = ST * P12;
   const Re L[2] = {re_div(-(BPC - SP), DV2), re_div(-(BPC + SP), DV2)};
-  bool any = false;
+  bool any = false, nan_lb = false;
 #pragma unroll
   for (int k = 0; k < 2; ++k) {
     const Re l = L[k];
@@ -124,8 +124,9 @@ __device__ __forceinline__ CandBound tri_screen(Re e12, Re e13, Re e23, Re p1, R
     any = true;
     r.lb = fminf(r.lb, re_lo(V));
     if (cond_certain && acc && re_lo(Q) >= 0.f) r.ub = fminf(r.ub, re_hi(V));
-    if (isnan(re_lo(V))) r.lb = NAN;
+    if (isnan(re_lo(V))) nan_lb = true;  // an overflowed bound of either root: no bound at all
   }
+  if (nan_lb) r.lb = NAN;
   if (!any) r.some = CAND_NONE;
   return r;
 }

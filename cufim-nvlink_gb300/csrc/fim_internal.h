@@ -105,10 +105,12 @@ struct FimParams {
 void set_last_error(const char *msg);
 
 // ---- kernels (fim_kernels.cu) ----
-// FP64 metric + edge norms per tet scattered into the corner records.
+// FP64 metric + edge norms of tets [e0, e1) scattered into the corner
+// records; the first tet with a non-positive or non-finite speed or a
+// non-finite fibre lowers *bad to its index.
 cudaError_t launch_metric(const int32_t *tslots, const int64_t *cidx, const double *xyz,
-                          const double *fib, const double *cf, const double *ct, int64_t nT,
-                          double *cgeo, float *cgf, uint4 *crec, cudaStream_t stream);
+                          const double *fib, const double *cf, const double *ct, int64_t e0, int64_t e1,
+                          double *cgeo, float *cgf, uint4 *crec, unsigned long long *bad, cudaStream_t stream);
 // Persistent cooperative solve.
 cudaError_t launch_solve(const FimDev &d, const FimParams &p, int grid, int block, cudaStream_t stream);
 // Occupancy-derived grid size for the cooperative launch.

@@ -227,12 +227,17 @@ __device__ __forceinline__ float half_hi(uint32_t w) { return __half2float(__ush
 __global__ void fim_metric_kernel(const int32_t *__restrict__ tslots, const int64_t *__restrict__ cidx,
                                   const double *__restrict__ xyz, const double *__restrict__ fib,
                                   const double *__restrict__ cf, const double *__restrict__ ct,
-                                  int64_t nT, double *__restrict__ cgeo, float *__restrict__ cgf,
-                                  uint4 *__restrict__ crec)
+                                  int64_t e0, int64_t e1, double *__restrict__ cgeo, float *__restrict__ cgf,
+                                  uint4 *__restrict__ crec, unsigned long long *__restrict__ bad)
 {
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nT;
+  for (int64_t e = e0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < e1;
        e += (int64_t)gridDim.x * blockDim.x) {
     const double f0 = fib[3 * e + 0], f1 = fib[3 * e + 1], f2 = fib[3 * e + 2];
+    // the input check of fim_set_conduction: positive finite speeds, finite
+    // fibre; the first offending tet is reported
+    if (!(cf[e] > 0.0 && ct[e] > 0.0 && isfinite(cf[e]) && isfinite(ct[e]) && isfinite(f0) && isfinite(f1) &&
+          isfinite(f2)))
+      atomicMin(bad, (unsigned long long)e);
     const double fa = f0*f0, fb = f0*f1, fc = f0*f2, fd = f1*f1, fe = f1*f2, ff = f2*f2;
     const double vf = 1. / cf[e] / cf[e], vs = 1. / ct[e] / ct[e];
     const double M0 = vf*fa + vs*(1. - fa);
@@ -1123,14 +1128,15 @@ __global__ void __launch_bounds__(kThreads, 1) fim_solve_kernel(FimDev d, FimPar
 // launch wrappers
 
 cudaError_t launch_metric(const int32_t *tslots, const int64_t *cidx, const double *xyz,
-                          const double *fib, const double *cf, const double *ct, int64_t nT,
-                          double *cgeo, float *cgf, uint4 *crec, cudaStream_t stream)
+                          const double *fib, const double *cf, const double *ct, int64_t e0, int64_t e1,
+                          double *cgeo, float *cgf, uint4 *crec, unsigned long long *bad, cudaStream_t stream)
 {
-  if (nT <= 0) return cudaSuccess;
+  if (e1 <= e0) return cudaSuccess;
   const int block = 256;
-  int64_t grid = (nT + block - 1) / block;
+  int64_t grid = (e1 - e0 + block - 1) / block;
   if (grid > 152 * 64) grid = 152 * 64;
-  fim_metric_kernel<<<(unsigned)grid, block, 0, stream>>>(tslots, cidx, xyz, fib, cf, ct, nT, cgeo, cgf, crec);
+  fim_metric_kernel<<<(unsigned)grid, block, 0, stream>>>(tslots, cidx, xyz, fib, cf, ct, e0, e1, cgeo, cgf, crec,
+                                                          bad);
   return cudaGetLastError();
 }
 

@@ -67,12 +67,21 @@ struct DevBuf {
 
 void fimgb::set_last_error(const char *msg) { g_last_error = msg; }
 
+// fim_set_conduction uploads the field in up to kCondChunks pieces of at
+// least kCondChunkMin tets.
+constexpr int kCondChunks = 8;
+constexpr int64_t kCondChunkMin = int64_t(1) << 18;
+
 struct fim_solver {
   fim_opts opts{};
   int device = 0;
   cudaStream_t own_stream = nullptr;  // created by fim_create
   cudaStream_t stream = nullptr;      // working stream (own_stream unless fim_set_stream)
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // conduction upload: copy stream, one event per chunk (chunk copies
+  // overlap the metric kernel of the chunk before), first invalid tet
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t ev_dep = nullptr, ev_chunk[kCondChunks] = {};
   std::string err;
   int grid = 0, block = kSolveThreads;
 
@@ -96,6 +105,7 @@ struct fim_solver {
   DevBuf<float> cgf, phi_f;
   DevBuf<int32_t> nbr;
   DevBuf<double> fib, cf, ct;
+  DevBuf<unsigned long long> bad;  // first invalid tet of the last conduction upload
   // state
   DevBuf<double> phi, phi2;
   DevBuf<uint8_t> st, tst, dec;
@@ -150,6 +160,15 @@ extern "C" const char *fim_last_error(const fim_solver *s)
   return g_last_error.c_str();
 }
 
+static cudaError_t create_chunk_events(fim_solver *s)
+{
+  for (cudaEvent_t &ev : s->ev_chunk) {
+    const cudaError_t e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
 extern "C" int fim_create(const fim_opts *opts, fim_solver **out)
 {
   if (!out) return set_err(nullptr, FIM_ERR_INVALID_ARGUMENT, "fim_create: out is NULL");
@@ -173,6 +192,9 @@ extern "C" int fim_create(const fim_opts *opts, fim_solver **out)
   if ((e = cudaSetDevice(s->device)) != cudaSuccess ||
       (e = cudaStreamCreateWithFlags(&s->own_stream, cudaStreamNonBlocking)) != cudaSuccess ||
       (e = cudaEventCreate(&s->ev0)) != cudaSuccess || (e = cudaEventCreate(&s->ev1)) != cudaSuccess ||
+      (e = cudaStreamCreateWithFlags(&s->copy_stream, cudaStreamNonBlocking)) != cudaSuccess ||
+      (e = cudaEventCreateWithFlags(&s->ev_dep, cudaEventDisableTiming)) != cudaSuccess ||
+      (e = create_chunk_events(s)) != cudaSuccess || (e = s->bad.alloc(1)) != cudaSuccess ||
       (e = solve_grid_size(s->device, s->block, &s->grid)) != cudaSuccess || (e = s->ctl.alloc(1)) != cudaSuccess) {
     int rc = set_err(nullptr, FIM_ERR_CUDA, "fim_create: %s", cudaGetErrorString(e));
     fim_destroy(s);
@@ -195,8 +217,13 @@ extern "C" int fim_destroy(fim_solver *s)
   cudaSetDevice(s->device);
   if (s->stream) cudaStreamSynchronize(s->stream);
   if (s->own_stream) cudaStreamSynchronize(s->own_stream);
+  if (s->copy_stream) cudaStreamSynchronize(s->copy_stream);
   if (s->ev0) cudaEventDestroy(s->ev0);
   if (s->ev1) cudaEventDestroy(s->ev1);
+  if (s->ev_dep) cudaEventDestroy(s->ev_dep);
+  for (cudaEvent_t ev : s->ev_chunk)
+    if (ev) cudaEventDestroy(ev);
+  if (s->copy_stream) cudaStreamDestroy(s->copy_stream);
   if (s->own_stream) cudaStreamDestroy(s->own_stream);
   s->own_stream = nullptr;
   s->stream = nullptr;
@@ -466,18 +493,55 @@ extern "C" int fim_set_mesh(fim_solver *s, int64_t nV, const double *xyz, int64_
   return FIM_OK;
 }
 
-static int run_metric(fim_solver *s)
+// Uploads a conduction field and runs the metric kernel.  The arrays (host
+// or device, by `host`) are copied over the copy stream in chunks, and each
+// chunk's metric launch waits only for its own copy, so the transfers
+// overlap the FP64 metric work.  The
+// kernel also checks the field (positive finite speeds, finite fibres): on a
+// bad tet the call fails and the solver has no conduction until a later call
+// succeeds.
+static int run_metric(fim_solver *s, const double *fib, const double *cf, const double *ct, bool host,
+                      const char *who)
 {
-  CUDA_TRY(s, cudaEventRecord(s->ev0, s->stream));
-  CUDA_TRY(s, launch_metric(s->tslots.p, s->cidx.p, s->xyz.p, s->fib.p, s->cf.p, s->ct.p, s->nT, s->cgeo.p, s->cgf.p,
-                            s->crec.p, s->stream));
+  const int64_t nT = s->nT;
+  const int nch = (int)std::max<int64_t>(1, std::min<int64_t>(kCondChunks, nT / kCondChunkMin));
+  const cudaMemcpyKind kind = host ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+  cudaStream_t cs = s->copy_stream;
+  s->have_cond = false;
+  s->solved = false;
+  CUDA_TRY(s, cudaMemsetAsync(s->bad.p, 0xff, sizeof(unsigned long long), s->stream));
+  // the copies overwrite arrays that earlier work on the working stream may read
+  CUDA_TRY(s, cudaEventRecord(s->ev_dep, s->stream));
+  CUDA_TRY(s, cudaStreamWaitEvent(cs, s->ev_dep, 0));
+  for (int i = 0; i < nch; ++i) {
+    const int64_t e0 = nT * i / nch, e1 = nT * (i + 1) / nch;
+    CUDA_TRY(s, cudaMemcpyAsync(s->fib.p + 3 * e0, fib + 3 * e0, sizeof(double) * 3 * (e1 - e0), kind, cs));
+    CUDA_TRY(s, cudaMemcpyAsync(s->cf.p + e0, cf + e0, sizeof(double) * (e1 - e0), kind, cs));
+    CUDA_TRY(s, cudaMemcpyAsync(s->ct.p + e0, ct + e0, sizeof(double) * (e1 - e0), kind, cs));
+    CUDA_TRY(s, cudaEventRecord(s->ev_chunk[i], cs));
+    CUDA_TRY(s, cudaStreamWaitEvent(s->stream, s->ev_chunk[i], 0));
+    if (i == 0) CUDA_TRY(s, cudaEventRecord(s->ev0, s->stream));
+    CUDA_TRY(s, launch_metric(s->tslots.p, s->cidx.p, s->xyz.p, s->fib.p, s->cf.p, s->ct.p, e0, e1, s->cgeo.p,
+                              s->cgf.p, s->crec.p, s->bad.p, s->stream));
+  }
   CUDA_TRY(s, cudaEventRecord(s->ev1, s->stream));
   CUDA_TRY(s, cudaEventSynchronize(s->ev1));
   float ms = 0.f;
   cudaEventElapsedTime(&ms, s->ev0, s->ev1);
   s->stats.metric_ms = ms;
+  unsigned long long bad = 0;
+  CUDA_TRY(s, cudaMemcpy(&bad, s->bad.p, sizeof bad, cudaMemcpyDeviceToHost));
+  if (bad < (unsigned long long)nT) {
+    const int64_t e = (int64_t)bad;
+    double v[5] = {0.0, 0.0, 0.0, 0.0, 0.0};  // cf, ct, fibre
+    CUDA_TRY(s, cudaMemcpy(v, s->cf.p + e, sizeof(double), cudaMemcpyDeviceToHost));
+    CUDA_TRY(s, cudaMemcpy(v + 1, s->ct.p + e, sizeof(double), cudaMemcpyDeviceToHost));
+    CUDA_TRY(s, cudaMemcpy(v + 2, s->fib.p + 3 * e, 3 * sizeof(double), cudaMemcpyDeviceToHost));
+    if (!(v[0] > 0.0) || !(v[1] > 0.0) || !std::isfinite(v[0]) || !std::isfinite(v[1]))
+      return set_err(s, FIM_ERR_INVALID_ARGUMENT, "%s: tet %lld has speed cf=%g ct=%g", who, (long long)e, v[0], v[1]);
+    return set_err(s, FIM_ERR_INVALID_ARGUMENT, "%s: tet %lld has a non-finite fibre", who, (long long)e);
+  }
   s->have_cond = true;
-  s->solved = false;
   return FIM_OK;
 }
 
@@ -486,27 +550,8 @@ extern "C" int fim_set_conduction(fim_solver *s, const double *fib, const double
   if (!s) return set_err(nullptr, FIM_ERR_INVALID_ARGUMENT, "fim_set_conduction: solver is NULL");
   if (!s->have_mesh) return set_err(s, FIM_ERR_NOT_READY, "fim_set_conduction: no mesh");
   if (!fib || !cf || !ct) return set_err(s, FIM_ERR_INVALID_ARGUMENT, "fim_set_conduction: NULL array");
-  // first tet with a bad speed / fibre (parallel scan, then the message of the first)
-  int64_t bad = s->nT;
-#pragma omp parallel for reduction(min : bad) schedule(static)
-  for (int64_t e = 0; e < s->nT; ++e) {
-    const bool ok = cf[e] > 0.0 && ct[e] > 0.0 && std::isfinite(cf[e]) && std::isfinite(ct[e]) &&
-                    std::isfinite(fib[3 * e]) && std::isfinite(fib[3 * e + 1]) && std::isfinite(fib[3 * e + 2]);
-    if (!ok && e < bad) bad = e;
-  }
-  if (bad < s->nT) {
-    const int64_t e = bad;
-    if (!(cf[e] > 0.0) || !(ct[e] > 0.0) || !std::isfinite(cf[e]) || !std::isfinite(ct[e]))
-      return set_err(s, FIM_ERR_INVALID_ARGUMENT, "fim_set_conduction: tet %lld has speed cf=%g ct=%g",
-                     (long long)e, cf[e], ct[e]);
-    return set_err(s, FIM_ERR_INVALID_ARGUMENT, "fim_set_conduction: tet %lld has a non-finite fibre",
-                   (long long)e);
-  }
   CUDA_TRY(s, cudaSetDevice(s->device));
-  CUDA_TRY(s, cudaMemcpyAsync(s->fib.p, fib, sizeof(double) * 3 * s->nT, cudaMemcpyHostToDevice, s->stream));
-  CUDA_TRY(s, cudaMemcpyAsync(s->cf.p, cf, sizeof(double) * s->nT, cudaMemcpyHostToDevice, s->stream));
-  CUDA_TRY(s, cudaMemcpyAsync(s->ct.p, ct, sizeof(double) * s->nT, cudaMemcpyHostToDevice, s->stream));
-  return run_metric(s);
+  return run_metric(s, fib, cf, ct, true, "fim_set_conduction");
 }
 
 extern "C" int fim_set_conduction_device(fim_solver *s, const double *d_fib, const double *d_cf, const double *d_ct)
@@ -515,10 +560,7 @@ extern "C" int fim_set_conduction_device(fim_solver *s, const double *d_fib, con
   if (!s->have_mesh) return set_err(s, FIM_ERR_NOT_READY, "fim_set_conduction_device: no mesh");
   if (!d_fib || !d_cf || !d_ct) return set_err(s, FIM_ERR_INVALID_ARGUMENT, "fim_set_conduction_device: NULL array");
   CUDA_TRY(s, cudaSetDevice(s->device));
-  CUDA_TRY(s, cudaMemcpyAsync(s->fib.p, d_fib, sizeof(double) * 3 * s->nT, cudaMemcpyDeviceToDevice, s->stream));
-  CUDA_TRY(s, cudaMemcpyAsync(s->cf.p, d_cf, sizeof(double) * s->nT, cudaMemcpyDeviceToDevice, s->stream));
-  CUDA_TRY(s, cudaMemcpyAsync(s->ct.p, d_ct, sizeof(double) * s->nT, cudaMemcpyDeviceToDevice, s->stream));
-  return run_metric(s);
+  return run_metric(s, d_fib, d_cf, d_ct, false, "fim_set_conduction_device");
 }
 
 extern "C" int fim_set_stimuli(fim_solver *s, int64_t n, const int64_t *vertices, const double *t0)

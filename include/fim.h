@@ -92,9 +92,16 @@ int fim_set_mesh(fim_solver *s, int64_t n_vertices, const double *xyz, int64_t n
  * M = cf^-2 f f^T + ct^-2 (I - f f^T) and its six squared edge norms are
  * computed on the GPU (compute_velocity_tensor_f3 + compute_geo,
  * types.h:173-188, types.cpp:227-257; the reference hard-codes fibre (1,0,0)
- * and 0.6 there, vtk.cpp:99-101, types.cpp:231). */
+ * and 0.6 there, vtk.cpp:99-101, types.cpp:231).  The arrays are uploaded
+ * in chunks whose transfers overlap the metric kernel (pinned host memory
+ * lets them run asynchronously) and are read until the call returns.  The
+ * GPU checks the field: a tet with a non-positive or non-finite speed or a
+ * non-finite fibre fails the call with FIM_ERR_INVALID_ARGUMENT, naming the
+ * first such tet, and the solver then has no conduction until a later call
+ * succeeds. */
 int fim_set_conduction(fim_solver *s, const double *fib, const double *cf, const double *ct);
-/* Same, with device pointers (already resident in HBM on the solver's device). */
+/* Same, with device pointers (already resident in HBM on the solver's
+ * device), with the same check. */
 int fim_set_conduction_device(fim_solver *s, const double *d_fib, const double *d_cf,
                               const double *d_ct);
 
