@@ -38,8 +38,14 @@ import numpy as np  # noqa: E402
 SLAB_CELLS = (266, 93, 40)
 # DRAM bytes (read + write) of one fim_solve_kernel launch per vertex update,
 # from ncu dram__bytes_read.sum + dram__bytes_write.sum on this workload
-# (7.755 GB for 4,689,493 vertex updates; profiles/fim_solve_kernel_slab266x93x40_launches.md)
-NCU_DRAM_BYTES_PER_VERTEX_UPDATE = 7.755e9 / 4689493
+# (4.185 GB for 4,689,493 vertex updates; profiles/fim_solve_kernel_slab266x93x40_launches.md)
+NCU_DRAM_BYTES_PER_VERTEX_UPDATE = 4.185e9 / 4689493
+
+
+def metric_launches(nT):
+    """fim_metric_kernel launches per conduction upload: the field goes up in
+    up to 8 chunks of at least 2^18 tets (fim_solver.cpp, run_metric)."""
+    return max(1, min(8, nT >> 18))
 METRICS = {
     "slab": "slab solves/s (1.03M-vertex anisotropic FIM, bit-exact vs FP64 oracle)",
     "cube": "cube solves/s (9,261-vertex plain FIM, bit-exact vs FP64 oracle)",
@@ -95,7 +101,7 @@ def workload(args):
                      "ct 0.24 mm/ms, 2 mm scar x0.1, 5 surface stimuli t0~U[0,10] ms; one submesh, "
                      "one endless window"),
         "vertices": nV, "tets": nT, "seed": 2,
-        "l2": "inputs larger than L2 (corner records 128 B x 4T = 3.0 GB)",
+        "l2": "inputs larger than L2 (corner records 112 B x 4T = 2.7 GB)",
         "parallelism": "replicas",
     }
     return case, cfg
@@ -323,7 +329,7 @@ def run_mine(args):
                               "latency of its per-batch phase chain (FP64 solves, block barriers), not by HBM")},
         "e2e": {"value": world * e2e_steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
-        "gpu_launches": 2 * args.steps,
+        "gpu_launches": (metric_launches(nT) + 1) * args.steps,
         "clocks": clk,
     }
     if world == 1 and not args.no_cpu_baseline:

@@ -479,7 +479,7 @@ extern "C" int fim_mlp_create(int device, uint64_t seed, fim_mlp **out)
   int rc = FIM_OK;
   auto fail = [&](int code) { fim_mlp_destroy(m); return code; };
   cudaError_t e;
-  if ((e = cudaStreamCreateWithFlags(&m->st, cudaStreamNonBlocking)) != cudaSuccess ||
+  if ((e = cudaStreamCreateWithFlags(&m->st, cudaStreamDefault)) != cudaSuccess ||
       (e = cudaMalloc(&m->P, sizeof(float) * kMlpParams)) != cudaSuccess ||
       (e = cudaMalloc(&m->G, sizeof(float) * kMlpParams)) != cudaSuccess ||
       (e = cudaMalloc(&m->M, sizeof(float) * kMlpParams)) != cudaSuccess ||

@@ -75,7 +75,7 @@ constexpr int64_t kCondChunkMin = int64_t(1) << 18;
 struct fim_solver {
   fim_opts opts{};
   int device = 0;
-  cudaStream_t own_stream = nullptr;  // created by fim_create
+  cudaStream_t own_stream = nullptr;  // created by fim_create (blocking: ordered after legacy-stream work)
   cudaStream_t stream = nullptr;      // working stream (own_stream unless fim_set_stream)
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   // conduction upload: copy stream, one event per chunk (chunk copies
@@ -190,9 +190,9 @@ extern "C" int fim_create(const fim_opts *opts, fim_solver **out)
   s->opts = o;
   s->device = o.device;
   if ((e = cudaSetDevice(s->device)) != cudaSuccess ||
-      (e = cudaStreamCreateWithFlags(&s->own_stream, cudaStreamNonBlocking)) != cudaSuccess ||
+      (e = cudaStreamCreateWithFlags(&s->own_stream, cudaStreamDefault)) != cudaSuccess ||
       (e = cudaEventCreate(&s->ev0)) != cudaSuccess || (e = cudaEventCreate(&s->ev1)) != cudaSuccess ||
-      (e = cudaStreamCreateWithFlags(&s->copy_stream, cudaStreamNonBlocking)) != cudaSuccess ||
+      (e = cudaStreamCreateWithFlags(&s->copy_stream, cudaStreamDefault)) != cudaSuccess ||
       (e = cudaEventCreateWithFlags(&s->ev_dep, cudaEventDisableTiming)) != cudaSuccess ||
       (e = create_chunk_events(s)) != cudaSuccess || (e = s->bad.alloc(1)) != cudaSuccess ||
       (e = solve_grid_size(s->device, s->block, &s->grid)) != cudaSuccess || (e = s->ctl.alloc(1)) != cudaSuccess) {

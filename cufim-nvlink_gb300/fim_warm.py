@@ -95,14 +95,21 @@ def evaluate(mlp, maps, torch):
 
 
 def warm_solve(solver, mlp, m, torch, inflate=1.05):
-    """Solve map m from the inflated prediction; returns (times, stats, start)."""
+    """Solve map m from the inflated prediction; returns (times, stats, start).
+
+    The start is clamped to the earliest stimulus time: FIM only ever lowers
+    a time, so a start below every stimulus (the network can predict negative
+    times near a stimulus) never settles and the solve runs into its
+    iteration cap -- the reference's algorithm does the same from such a
+    start."""
     c = m.case
     solver.set_mesh(c["xyz"], c["tets"])
     solver.set_conduction(c["fib"], c["cf"], c["ct"])
     solver.set_stimuli(c["seed_v"], c["seed_t"])
-    start = (predict_times(mlp, m, torch) * inflate).contiguous()
+    t_first = float(np.min(c["seed_t"]))
+    start = torch.clamp(predict_times(mlp, m, torch) * inflate, min=t_first).contiguous()
     solver.set_warm_start(start.data_ptr())
-    solver.solve()
+    solver.solve(torch.cuda.current_stream().cuda_stream)  # after the kernels that wrote `start`
     phi = solver.times(with_state=False)
     st = solver.stats()
     solver.set_warm_start(None)

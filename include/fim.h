@@ -16,6 +16,11 @@
  *  - Times, lengths and speeds are in any consistent unit system (the
  *    reference's files use um, um/us and us).
  *  - A solver object is used from one host thread at a time.
+ *  - Device arrays passed in must be complete when the call is made.  The
+ *    library's own streams are blocking streams, so its work is ordered
+ *    after earlier work on the legacy default stream (PyTorch's default
+ *    stream); data written on any other stream must be synchronised by the
+ *    caller, or that stream passed where a call takes one (fim_solve).
  *  - Solve semantics are those of the reference's CudaSolverFIM::solve with
  *    every tet in one submesh: windows of length dt, n_steps of them,
  *    narrow/next/frozen/tail states, the front-width rule and the APD reset
@@ -225,8 +230,11 @@ int fim_mlp_predict(fim_mlp *m, int64_t n, const void *d_features, float *d_out)
  * largest stimulus distance, the unit of the distance feature and of the
  * normalised times the network predicts. */
 int fim_features(fim_solver *s, void *d_features, float *time_scale);
-/* Start times (device, FP64 [n_vertices], kept by the caller until the
- * solve) for the next solves; NULL restores the cold start. */
+/* Start times (device, FP64 [n_vertices], complete before and kept by the
+ * caller until the solve) for the next solves; NULL restores the cold start.
+ * FIM only lowers times, so a start below the true time of a vertex stays
+ * wrong, and a start below the earliest stimulus time can keep the
+ * iteration from settling (it then stops at max_iterations). */
 int fim_set_warm_start(fim_solver *s, const double *d_phi_init);
 
 /* Reference-compatible files.  fim_vtk_* read/write the legacy ASCII VTK

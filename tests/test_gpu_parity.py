@@ -59,6 +59,37 @@ def test_anisotropic_slab_bit_exact(F, O):
     assert stats["iterations"] == it_o
 
 
+def test_warm_start_bit_exact(F, O):
+    """fim_set_warm_start: every vertex starts narrow at its given time (here
+    1.05 x the cold result; unreached vertices stay far).  The oracle runs the
+    same FIM seeded with every vertex at its start time, the stimuli after
+    them so that their own times win, as they do on the GPU."""
+    import fim_mesh
+    torch = pytest.importorskip("torch")
+    c = fim_mesh.slab_case(cells=(40, 14, 6), size=(20.0, 7.0, 3.0), seed=5)
+    nV = c["xyz"].shape[0]
+    cold, _, _ = F.solve_case(c)
+    start = np.where(cold < F.INF, 1.05 * cold, F.INF)
+    d_start = torch.from_numpy(start).cuda()
+    torch.cuda.synchronize()
+    with F.Solver() as s:
+        s.set_mesh(c["xyz"], c["tets"])
+        s.set_conduction(c["fib"], c["cf"], c["ct"])
+        s.set_stimuli(c["seed_v"], c["seed_t"])
+        s.set_warm_start(d_start.data_ptr())
+        s.solve()
+        phi, st = s.times()
+        it = s.stats()["iterations"]
+    slots, _, _, _ = O.reference_slots(nV, c["tets"], None)
+    geo = O.metric_geo(slots, c["xyz"], c["fib"], c["cf"], c["ct"])
+    sv = np.concatenate([np.arange(nV), c["seed_v"]])
+    st0 = np.concatenate([start, c["seed_t"]])
+    keep = st0 < F.INF
+    phi_o, st_o, it_o, _ = O.solve_pure(nV, slots, geo, sv[keep], st0[keep])
+    assert_identical(phi, st, phi_o, st_o)
+    assert it == it_o
+
+
 def _ut(O, tag_key):
     ut = np.load(os.path.join(GOLDEN, "ut_mesh.npz"))
     xyz, tets = ut["xyz"], np.sort(ut["tets"], axis=1)
