@@ -36,6 +36,55 @@ namespace fimgb {
 // ---------------------------------------------------------------------------
 // local solver, FP64 with the reference's float-typed triangle intermediates
 
+// Exact float <-> double conversions and FP64 sign tests from the bit
+// patterns (IEEE 754 binary32 / binary64), on the integer pipes: on GB300 a
+// conversion or an FP64 comparison occupies the FP64 pipe like an FP64
+// multiply.  Operands outside the normal range take the hardware
+// instruction.
+
+// (double)f, exact
+__device__ __forceinline__ double f2d(float f)
+{
+  const uint32_t u = __float_as_uint(f);
+  const uint32_t e = (u >> 23) & 0xffu;
+  if (e - 1u < 254u)  // normal: rebias the exponent, widen the fraction
+    return __longlong_as_double((long long)(((unsigned long long)(u & 0x80000000u) << 32) |
+                                            ((unsigned long long)(e + 896u) << 52) |
+                                            ((unsigned long long)(u & 0x7fffffu) << 29)));
+  return (double)f;  // zero, subnormal, infinity, NaN
+}
+
+// (float)x, round to nearest, ties to even
+__device__ __forceinline__ float d2f(double x)
+{
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const uint32_t e = (uint32_t)(b >> 52) & 0x7ffu;
+  if (e - 897u < 254u) {  // the float is normal, or rounds up to infinity
+    const uint32_t frac = (uint32_t)(b >> 29) & 0x7fffffu;
+    const uint32_t rest = (uint32_t)b & 0x1fffffffu;  // the 29 bits dropped
+    uint32_t r = ((e - 896u) << 23) | frac;
+    r += (rest > 0x10000000u || (rest == 0x10000000u && (frac & 1u))) ? 1u : 0u;  // carries into the exponent
+    return __uint_as_float(r | ((uint32_t)(b >> 32) & 0x80000000u));
+  }
+  return (float)x;  // zero, subnormal result, infinity, NaN
+}
+
+// x > 0 (false for zeros and NaN)
+__device__ __forceinline__ bool dgt0(double x)
+{
+  return (unsigned long long)__double_as_longlong(x) - 1ull < 0x7ff0000000000000ull;
+}
+// 0 < x < 1
+__device__ __forceinline__ bool din01(double x)
+{
+  return (unsigned long long)__double_as_longlong(x) - 1ull < 0x3fefffffffffffffull;
+}
+// x < 0 (false for zeros and NaN)
+__device__ __forceinline__ bool dlt0(double x)
+{
+  return (unsigned long long)__double_as_longlong(x) - 0x8000000000000001ull < 0x7ff0000000000000ull;
+}
+
 // solve_tri_cu, cuda_fim.h:1256-1300
 __device__ __forceinline__ double tri_ref(double e12, double e13, double e23, double p1, double p2)
 {
@@ -43,21 +92,24 @@ __device__ __forceinline__ double tri_ref(double e12, double e13, double e23, do
   const double b = -0.5 * (e12 + e23 - e13);
   const double c = e12;
   const double p12 = p2 - p1;
-  float dv = (float)(p12 * p12 - c);
-  const float sv = (float)((double)dv * (b * b - a * c));
+  // the reference's float casts as d2f / f2d (same values)
+  float dv = d2f(p12 * p12 - c);
+  const float sv = d2f(f2d(dv) * (b * b - a * c));
   // the reference compares the float intermediates after widening them to
   // double; comparing the floats themselves gives the same answers (NaN too)
   // without the FP64 conversions
   if (dv != 0.f && sv >= 0.f) {
-    dv = (float)(c * (double)dv);
+    dv = d2f(c * f2d(dv));
     const float st = sqrtf(sv);
-    const float l1 = (float)(-(b * p12 * p12 - b * c - (double)st * p12) / (double)dv);
-    const float l2 = (float)(-(b * p12 * p12 - b * c + (double)st * p12) / (double)dv);
-    float r1 = (float)(p2 - (double)l1 * p12 + sqrt(a + 2.0 * (double)l1 * b + (double)(l1 * l1) * c));
+    const double dst = f2d(st), ddv = f2d(dv);
+    const float l1 = d2f(-(b * p12 * p12 - b * c - dst * p12) / ddv);
+    const float l2 = d2f(-(b * p12 * p12 - b * c + dst * p12) / ddv);
+    const double dl1 = f2d(l1), dl2 = f2d(l2);
+    float r1 = d2f(p2 - dl1 * p12 + sqrt(a + 2.0 * dl1 * b + f2d(l1 * l1) * c));
     if (!((l1 >= 0.f) && (l1 <= 1.f))) r1 = (float)FIM_INF;
-    float r2 = (float)(p2 - (double)l2 * p12 + sqrt(a + 2.0 * (double)l2 * b + (double)(l2 * l2) * c));
+    float r2 = d2f(p2 - dl2 * p12 + sqrt(a + 2.0 * dl2 * b + f2d(l2 * l2) * c));
     if (!((l2 >= 0.f) && (l2 <= 1.f))) r2 = (float)FIM_INF;
-    return (double)fminf(r1, r2);
+    return f2d(fminf(r1, r2));
   }
   return FIM_INF;
 }
@@ -103,53 +155,13 @@ __device__ __forceinline__ double tet_ref(double e13, double e23, double e34, do
   return fmin(ra, rb);
 }
 
-// One of the two roots of tet_ref: second = false gives its "a" value
-// (pa + sqt X), true its "b" value (pa - sqt X, written as pa + (-(sqt X)),
-// which IEEE arithmetic rounds identically), so two lanes of a warp run one
-// instruction stream and tet_ref's result is the fmin of their values.
-__device__ __forceinline__ double tet_ref_root(double e13, double e23, double e34, double e12, double e14,
-                                               double e24, double p1, double p2, double p3, bool second)
-{
-  const double a = e13;
-  const double b = 0.5 * (e23 + e13 - e12);
-  const double c = -0.5 * (e34 + e13 - e14);
-  const double d = e23;
-  const double e = -0.5 * (e34 + e23 - e24);
-  const double f = e34;
-  const double q13 = p3 - p1;
-  const double q23 = p3 - p2;
-
-  const double sqt =
-    -e*e*c*d*d + a*d*d*d*d - (b*b*c - a*c*c)*f*f + ((b*b - a*c)*f*f -
-    (e*e*c - a*d*d - 2.*(e*c - b*d)*e)*f)*q13*q13 - 2.*(e*e*c*d -
-    2.*e*b*d*d + a*d*d*d + (b*b - a*c)*d*f)*q13*q23 + (e*e*c*c -
-    2.*e*b*c*d + a*c*d*d + (b*b*c - a*c*c)*f)*q23*q23 + 2.*(e*c*d*d -
-    b*d*d*d)*e + (e*e*c*c + (b*b - 2.*a*c)*d*d - 2.*(e*c*c - b*c*d)*e)*f;
-
-  if (sqt < 0.) return FIM_INF;
-
-  const double pa = e*c*d*d - b*d*d*d + (e*c - b*d)*f*q13*q13 - 2.*(e*c*d - b*d*d)*q13*q23 +
-                    (e*c*c - b*c*d)*q23*q23 - (e*c*c - b*c*d)*f;
-  const double pb = (d*d*d*d - 2.*c*d*d*f + c*c*f*f + (d*d*f - c*f*f)*q13*q13 -
-                     2.*(d*d*d - c*d*f)*q13*q23 + (c*d*d - c*c*f)*q23*q23);
-
-  const double sx = sqt*(d*q13 - c*q23);
-  const double l2 = (pa + (second ? -sx : sx))/pb;
-  const double l1 = -((f*l2 + e)*q13 - (d*l2 + b)*q23)/(d*q13 - c*q23);
-  const double l3 = 1 - l1 - l2;
-  double r = FIM_INF;
-  if ((l1 > 0. && l1 < 1.) && (l2 > 0. && l2 < 1.) && l3 > 0.)
-    r = l1*p1 + l2*p2 + l3*p3 + sqrt(a + 2.*l1*b + l1*l1*c + 2.*l1*l2*d + 2.*l2*e + l2*l2*f);
-  return r;
-}
-
 // The same tet solve with its long FP64 prefix (b, c, e, q13, q23, sqt, pa,
 // pb, sqt*X) spread over a group of kDagLanes lanes: the generated level
 // program (gen_tet_dag.py) gives each lane one DFMA per level on operands in
 // the group's scratch S, so the prefix costs kDagLevels dependent FP64
 // instructions instead of one per node.  The results are bit-identical to
-// tet_ref_root (every node is one correctly rounded operation of the source's
-// own expression tree).
+// tet_ref (every node is one correctly rounded operation of the source's own
+// expression tree).
 #include "tet_dag.inc"
 
 __device__ __forceinline__ double flip_sign(double x, uint32_t flip)
@@ -172,7 +184,11 @@ __device__ __forceinline__ void tet_dag_prefix(double *S, int gl)
   }
 }
 
-// The root part of tet_ref_root on the prefix in S (second: its "b" root).
+// One root of tet_ref from the prefix in S: second = false gives its "a"
+// value (pa + sqt X), true its "b" value (pa - sqt X, written as
+// pa + (-(sqt X)), which IEEE arithmetic rounds identically), so two lanes
+// run one instruction stream and tet_ref's result is the fmin of their
+// values.  The sign tests run on the integer pipes (dlt0, din01, dgt0).
 __device__ __forceinline__ double tet_root_tail(const double *S, bool second)
 {
   const double a = S[kDagLeafE13], d = S[kDagLeafE13 + 1], f = S[kDagLeafE13 + 2];
@@ -180,13 +196,13 @@ __device__ __forceinline__ double tet_root_tail(const double *S, bool second)
   const double p1 = S[kDagLeafP1], p2 = S[kDagLeafP1 + 1], p3 = S[kDagLeafP1 + 2];
   const double q13 = S[kDagOut_q13], q23 = S[kDagOut_q23];
   const double sqt = S[kDagOut_sqt];
-  if (sqt < 0.) return FIM_INF;
+  if (dlt0(sqt)) return FIM_INF;
   const double pa = S[kDagOut_pa], pb = S[kDagOut_pb], sx = S[kDagOut_sx], X = S[kDagOut_X];
   const double l2 = (pa + (second ? -sx : sx))/pb;
   const double l1 = -((f*l2 + e)*q13 - (d*l2 + b)*q23)/X;
   const double l3 = 1 - l1 - l2;
   double r = FIM_INF;
-  if ((l1 > 0. && l1 < 1.) && (l2 > 0. && l2 < 1.) && l3 > 0.)
+  if (din01(l1) && din01(l2) && dgt0(l3))
     r = l1*p1 + l2*p2 + l3*p3 + sqrt(a + 2.*l1*b + l1*l1*c + 2.*l1*l2*d + 2.*l2*e + l2*l2*f);
   return r;
 }
