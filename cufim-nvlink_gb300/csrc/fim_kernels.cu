@@ -69,6 +69,23 @@ __device__ __forceinline__ float d2f(double x)
   return (float)x;  // zero, subnormal result, infinity, NaN
 }
 
+// (float)(x * 2^-s) for |s| <= 60, round to nearest, ties to even: the
+// scaling is an exponent change, exact whenever the scaled double is normal
+__device__ __forceinline__ float d2f_pow2(double x, int s)
+{
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const int e = (int)((b >> 52) & 0x7ffu);
+  const int es = e - s;  // biased exponent of x * 2^-s
+  if (e != 0 && e != 0x7ff && (uint32_t)(es - 897) < 254u) {
+    const uint32_t frac = (uint32_t)(b >> 29) & 0x7fffffu;
+    const uint32_t rest = (uint32_t)b & 0x1fffffffu;
+    uint32_t r = ((uint32_t)(es - 896) << 23) | frac;
+    r += (rest > 0x10000000u || (rest == 0x10000000u && (frac & 1u))) ? 1u : 0u;
+    return __uint_as_float(r | ((uint32_t)(b >> 32) & 0x80000000u));
+  }
+  return (float)(x * ldexp(1.0, -s));
+}
+
 // x > 0 (false for zeros and NaN)
 __device__ __forceinline__ bool dgt0(double x)
 {
@@ -284,7 +301,6 @@ __global__ void fim_metric_kernel(const int32_t *__restrict__ tslots, const int6
     int ks = ex & ~1;
     const bool ok = isfinite(gmax) && gmax > 0.0 && ks <= 50 && ks >= -50;
     if (!ok) ks = 0;
-    const double sg = ldexp(1.0, -ks);
     const float tk = ldexpf(1.f, ks / 2);
     // FP32 copies of the edge norms (scaled) and of the three edge lengths
     // towards each corner: sqrtf of the scaled norm times 2^(k/2), within
@@ -293,7 +309,7 @@ __global__ void fim_metric_kernel(const int32_t *__restrict__ tslots, const int6
     float gsc[6], len[6];
 #pragma unroll
     for (int k = 0; k < 6; ++k) {
-      gsc[k] = (float)(g[k] * sg);
+      gsc[k] = d2f_pow2(g[k], ks);  // (float)(g * 2^-ks)
       len[k] = sqrtf(gsc[k]) * tk;
     }
 #pragma unroll
@@ -797,13 +813,27 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
 #pragma unroll
         for (int i = 0; i < 4; ++i) lb[i] = sh.lbt[j][i];
       }
-      // triangle pairs (1,2), (2,3), (1,3) and the tet
+      // triangle pairs (1,2), (2,3), (1,3), appended together (one atomic
+      // per warp for the three), then the tet
+      bool need[3];
+      unsigned msk[3];
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
         const int a = k == 1 ? 1 : 0, b = k == 0 ? 1 : 2;
-        const bool need = in && ((m >> a) & 1u) && ((m >> b) & 1u) && !(lb[k] > bhi);
-        const int p = warp_append(&sh.ntri, need, lane);
-        if (p >= 0) {
+        need[k] = in && ((m >> a) & 1u) && ((m >> b) & 1u) && !(lb[k] > bhi);
+        msk[k] = __ballot_sync(FULL_MASK, need[k]);
+      }
+      const int n0 = __popc(msk[0]), n1 = __popc(msk[1]), n2 = __popc(msk[2]);
+      if (n0 + n1 + n2 > 0) {
+        int base = 0;
+        if (lane == 0) base = atomicAdd(&sh.ntri, n0 + n1 + n2);
+        base = __shfl_sync(FULL_MASK, base, 0);
+        const unsigned below = (1u << lane) - 1u;
+        const int first[3] = {base, base + n0, base + n0 + n1};  // the warp's pair-0 items, then 1, then 2
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          if (!need[k]) continue;
+          const int p = first[k] + __popc(msk[k] & below);
           if (p < kTriCap) {
             sh.tri[p] = (uint32_t)j | ((uint32_t)k << 16);
           } else {  // list full: screen here
