@@ -426,9 +426,9 @@ __device__ __forceinline__ double dunkey(unsigned long long k)
 constexpr int kThreads = kSolveThreads;  // threads per block of the solve kernel
 constexpr int kSlots = 128;         // vertices per batch (at most)
 constexpr int kCornerCap = 2560;    // corners per batch
-constexpr int kTriCap = kCornerCap * 3 / 2;  // triangle screens per batch (more are screened on the spot)
+constexpr int kTriCap = kCornerCap * 6 / 5;  // triangle screens per batch (more are screened on the spot)
 constexpr int kTetCap = kCornerCap; // tet screens per batch: never full
-constexpr int kQcap = 1024;         // exact solves queued per kind and batch
+constexpr int kQcap = 768;          // exact solves queued per kind and batch (more run on the spot)
 // Phase D runs the queued tets on at most kDagWarps warps, one group of
 // kDagLanes lanes per tet (scratch: kDagGroups * kDagSlots doubles).
 constexpr int kDagWarps = 7;
@@ -459,12 +459,14 @@ struct BatchSh {
   unsigned int bhi[kSlots];         // fkey of a float upper bound of the new time
   // per corner of the batch
   int32_t nb[kCornerCap][3];        // the other three vertices
-  float pf[kCornerCap][3];          // their float times
-  float sf[kCornerCap][3];          // float edge lengths sqrt(e14), sqrt(e24), sqrt(e34)
   union {
-    float lbt[kCornerCap][4];       // root-term bounds, then lower bounds of pairs (1,2), (2,3), (1,3) and tet
-    double dag[kDagGroups][kDagSlots];  // phase D: scratch of the tet prefix groups
+    struct {
+      float pf[kCornerCap][3];      // their float times
+      float sf[kCornerCap][3];      // float edge lengths sqrt(e14), sqrt(e24), sqrt(e34)
+    };
+    double dag[kDagGroups][kDagSlots];  // phase D (where pf and sf are dead): scratch of the tet prefix groups
   };
+  uint32_t hb[kCornerCap][2];       // root-term bounds of pairs (1,2), (2,3) | (1,3), tet: fp16 pairs rounded down
   uint8_t vm[kCornerCap];           // validity bits of the three neighbours
   uint8_t cs[kCornerCap];           // slot of the corner's vertex
   // compacted screen lists: item (corner j | pair k << 16)
@@ -477,8 +479,8 @@ struct BatchSh {
   int nslot;                        // vertices of the current batch
 };
 
-static_assert(sizeof(double) * kDagGroups * kDagSlots <= sizeof(float) * kCornerCap * 4,
-              "the tet prefix scratch must fit in the lower-bound array it overlays");
+static_assert(sizeof(double) * kDagGroups * kDagSlots <= sizeof(float) * kCornerCap * 6,
+              "the tet prefix scratch must fit in the arrays it overlays");
 
 // Queue item: slot (7 bits) | kind (2 bits) | corner index in the batch (23 bits).
 // kind: triangle pair 0..2 or 3 (tet) in queues 0 and 1, edge 0..2 in queue 2.
@@ -728,8 +730,8 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
       for (int r = 0; r < kPer; ++r) {
         const int j = jb + tid + r * kThreads;
         if (j < kept) {
-          sh.lbt[j][0] = half_lo(h0[r].w); sh.lbt[j][1] = half_hi(h0[r].w);
-          sh.lbt[j][2] = half_lo(h1[r].w); sh.lbt[j][3] = half_hi(h1[r].w);
+          sh.hb[j][0] = h0[r].w;
+          sh.hb[j][1] = h1[r].w;
           sh.nb[j][0] = (int32_t)h0[r].x; sh.nb[j][1] = (int32_t)h0[r].y; sh.nb[j][2] = (int32_t)h0[r].z;
           sh.sf[j][0] = __uint_as_float(h1[r].x); sh.sf[j][1] = __uint_as_float(h1[r].y);
           sh.sf[j][2] = __uint_as_float(h1[r].z);
@@ -760,18 +762,6 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
         if (m) ++n_filtered;
         if (!exact_all && ub < INFINITY) atomicMin(&sh.bhi[slot[r]], fkey(ub));
         sh.vm[j] = (uint8_t)m;
-        // lower bounds of the triangle pairs and the tet: min(times) + root-term bound
-        float lo[3], hi[3];
-#pragma unroll
-        for (int i = 0; i < 3; ++i) {
-          const Re P = re_in(pf[r][i]);
-          lo[i] = re_lo(P);
-          hi[i] = re_hi(P);
-        }
-        sh.lbt[j][0] = solve_lo(fminf(lo[0], lo[1]), fmaxf(hi[0], hi[1]), sh.lbt[j][0]);
-        sh.lbt[j][1] = solve_lo(fminf(lo[1], lo[2]), fmaxf(hi[1], hi[2]), sh.lbt[j][1]);
-        sh.lbt[j][2] = solve_lo(fminf(lo[0], lo[2]), fmaxf(hi[0], hi[2]), sh.lbt[j][2]);
-        sh.lbt[j][3] = solve_lo(fminf(lo[0], fminf(lo[1], lo[2])), fmaxf(hi[0], fmaxf(hi[1], hi[2])), sh.lbt[j][3]);
       }
     }
     // corners beyond kCornerCap (a single vertex with very many corners):
@@ -810,8 +800,19 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
         slot = sh.cs[j];
         m = sh.vm[j];
         bhi = funkey(sh.bhi[slot]);
+        // lower bounds of the triangle pairs and the tet: min(times) + root-term bound
+        float lo[3], hi[3];
 #pragma unroll
-        for (int i = 0; i < 4; ++i) lb[i] = sh.lbt[j][i];
+        for (int i = 0; i < 3; ++i) {
+          const Re P = re_in(sh.pf[j][i]);
+          lo[i] = re_lo(P);
+          hi[i] = re_hi(P);
+        }
+        const uint32_t w0 = sh.hb[j][0], w1 = sh.hb[j][1];
+        lb[0] = solve_lo(fminf(lo[0], lo[1]), fmaxf(hi[0], hi[1]), half_lo(w0));
+        lb[1] = solve_lo(fminf(lo[1], lo[2]), fmaxf(hi[1], hi[2]), half_hi(w0));
+        lb[2] = solve_lo(fminf(lo[0], lo[2]), fmaxf(hi[0], hi[2]), half_lo(w1));
+        lb[3] = solve_lo(fminf(lo[0], fminf(lo[1], lo[2])), fmaxf(hi[0], fmaxf(hi[1], hi[2])), half_hi(w1));
       }
       // triangle pairs (1,2), (2,3), (1,3), appended together (one atomic
       // per warp for the three), then the tet
