@@ -131,6 +131,78 @@ __device__ __forceinline__ CandBound tri_screen(Re e12, Re e13, Re e23, Re p1, R
   return r;
 }
 
+// Branch-free division and square root (hardware approximations, no
+// operand-range branches): __fdividef is within 2 ulp for divisors of
+// magnitude in [2^-126, 2^126] (elsewhere the result gets no bound: e = inf);
+// x rsqrtf(x) within 2.5 ulp for x >= 2^-126 (smaller x: value 0, error
+// 2^-63 = sqrt(2^-126)).  The extra error is covered by |v| 2^-21; the error
+// terms are raised by 2^-20 to stay upper bounds.
+#define FIM_RE_APPROX 0x1p-21f
+#define FIM_RE_UP 1.00000095367431640625f  // 1 + 2^-20
+__device__ __forceinline__ Re re_div_bf(Re a, Re b)
+{
+  const float ay = fabsf(b.v);
+  const float d = ay - b.e * FIM_RE_SAFE;
+  const float v = __fdividef(a.v, b.v);
+  const float prop = __fdividef(a.e + fabsf(v) * b.e, fmaxf(d, 0x1p-126f)) * FIM_RE_UP;
+  const float e = fmaf(fabsf(v), FIM_RE_U + FIM_RE_APPROX, prop + FIM_RE_TINY);
+  const bool ok = d > 0.f && ay >= 0x1p-126f && ay <= 0x1p126f;
+  return re_make(ok ? v : 0.f, ok ? e : INFINITY);
+}
+__device__ __forceinline__ float sqrt_up_bf(float x)  // an upper bound of sqrt(x), x >= 0
+{
+  const float y = fmaxf(x, 0x1p-126f);
+  return y * rsqrtf(y) * FIM_RE_UP * (1.f + 0x1p-21f);
+}
+__device__ __forceinline__ Re re_sqrt_bf(Re a)
+{
+  const float x = fmaxf(a.v, 0.f);
+  const bool big = x >= 0x1p-126f;
+  const float r = rsqrtf(fmaxf(x, 0x1p-126f));
+  const float v = big ? x * r : 0.f;
+  const float ea = a.e * FIM_RE_SAFE;
+  const float e = fminf(big ? ea * r * FIM_RE_UP * (1.f + 0x1p-21f) : INFINITY, sqrt_up_bf(ea)) + (big ? 0.f : 0x1p-63f);
+  return re_make(v, fmaf(v, FIM_RE_U + FIM_RE_APPROX, e + FIM_RE_TINY));
+}
+
+// tri_screen without branches (the same decisions, the two roots as
+// independent chains), for lanes that screen two pairs at once.
+__device__ __forceinline__ CandBound tri_screen_bf(Re e12, Re e13, Re e23, Re p1, Re p2)
+{
+  CandBound r;
+  const Re P12 = p2 - p1;
+  const Re A = e23, C = e12;
+  const Re B = re_scale((e12 + e23) - e13, -0.5f);
+  const Re DV = P12 * P12 - C;
+  const Re SV = DV * (B * B - A * C);
+  const bool none_sv = re_hi(SV) < 0.f;
+  const bool cond_certain = (re_lo(DV) > 0.f || re_hi(DV) < 0.f) && re_lo(SV) >= 0.f;
+  const Re DV2 = C * DV;
+  const Re ST = re_sqrt_bf(SV);
+  const Re BPC = (B * P12) * P12 - B * C;
+  const Re SP = ST * P12;
+  const Re L0 = re_div_bf(-(BPC - SP), DV2), L1 = re_div_bf(-(BPC + SP), DV2);
+  bool any = false, nan_lb = false;
+  float lb = INFINITY, ub = INFINITY;
+#pragma unroll
+  for (int k = 0; k < 2; ++k) {
+    const Re l = k == 0 ? L0 : L1;
+    const Re Q = (A + re_scale(l, 2.f) * B) + (l * l) * C;
+    const Re V = (p2 - l * P12) + re_sqrt_bf(Q);
+    const bool use = !(re_hi(l) < 0.f || re_lo(l) > 1.f) && !(re_hi(Q) < 0.f);
+    const bool acc = re_lo(l) >= 0.f && re_hi(l) <= 1.f;
+    const float vl = re_lo(V);
+    any = any || use;
+    nan_lb = nan_lb || (use && isnan(vl));
+    lb = use ? fminf(lb, vl) : lb;
+    ub = (use && cond_certain && acc && re_lo(Q) >= 0.f) ? fminf(ub, re_hi(V)) : ub;
+  }
+  r.some = (none_sv || !any) ? CAND_NONE : CAND_SOME;
+  r.lb = nan_lb ? NAN : lb;
+  r.ub = none_sv ? INFINITY : ub;
+  return r;
+}
+
 // solve_tet_cu with scaled edge norms g = e13, e23, e34, e12, e14, e24 (each
 // times 2^-k), true times p1..p3 and k.
 __device__ __forceinline__ CandBound tet_screen(const Re *g, Re p1, Re p2, Re p3, int k)

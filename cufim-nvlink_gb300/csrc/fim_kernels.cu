@@ -853,36 +853,81 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
     }
     __syncthreads();
 
-    // S: screens over the compacted lists, handed out in chunks of 32 items
-    // (one per lane) to whichever warp is free -- tets first, then triangles
-    // from the next chunk boundary, so that every chunk holds one kind; a
-    // solve whose lower bound does not exceed the current bhi is queued at
-    // once (bhi only decreases: phase D rechecks against the final bound)
+    // S: screens over the compacted lists, handed out in chunks to whichever
+    // warp is free -- tets first (32 per chunk, one per lane), then triangles
+    // from the next chunk boundary (64 per chunk: each lane screens two with
+    // the branch-free tri_screen_bf, so that the two chains interleave), so
+    // that every chunk holds one kind; a solve whose lower bound does not
+    // exceed the current bhi is queued at once (bhi only decreases: phase D
+    // rechecks against the final bound)
     {
       const int ntet = min(sh.ntet, kTetCap), ntri = min(sh.ntri, kTriCap);
       const int tri0 = (ntet + 31) & ~31;
       for (;;) {
+        // tet chunks of 32 items, then triangle chunks of 64 (two per lane)
         int ib = 0;
-        if (lane == 0) ib = atomicAdd(&sh.next_item, 32);
+        if (lane == 0) {
+          ib = atomicAdd(&sh.next_item, 32);
+          if (ib >= tri0) ib = tri0 + 2 * (ib - tri0);  // 32 claimed in the triangle range stand for 64
+        }
         ib = __shfl_sync(FULL_MASK, ib, 0);
         if (ib >= tri0 + ntri) break;
-        const int i = ib + lane;
-        const int qi = ib < tri0 ? 0 : 1;  // the same on every lane of the warp
-        bool need = false;
-        int kind = 0, slot = 0, j = 0;
-        float lb = 0.f;
-        if (qi == 0 ? i < ntet : i < tri0 + ntri) {
-          if (qi == 0) { j = (int)sh.tet[i]; kind = 3; }
-          else { const uint32_t it = sh.tri[i - tri0]; j = (int)(it & 0xffffu); kind = (int)(it >> 16); }
-          slot = sh.cs[j];
-          CandBound cb;
-          if (exact_all) { cb.some = CAND_SOME; cb.lb = NAN; cb.ub = INFINITY; }
-          else cb = qi == 0 ? tet_screen_sm(d, sh, j) : tri_screen_sm(d, sh, j, kind);
-          if (!exact_all && cb.some && cb.ub < INFINITY) atomicMin(&sh.bhi[slot], fkey(cb.ub));
-          lb = isnan(cb.lb) ? -INFINITY : cb.lb;
-          need = cb.some && !(lb > funkey(sh.bhi[slot]));
+        if (ib < tri0) {
+          const int i = ib + lane;
+          bool need = false;
+          int slot = 0, j = 0;
+          float lb = 0.f;
+          if (i < ntet) {
+            j = (int)sh.tet[i];
+            slot = sh.cs[j];
+            CandBound cb;
+            if (exact_all) { cb.some = CAND_SOME; cb.lb = NAN; cb.ub = INFINITY; }
+            else cb = tet_screen_sm(d, sh, j);
+            if (!exact_all && cb.some && cb.ub < INFINITY) atomicMin(&sh.bhi[slot], fkey(cb.ub));
+            lb = isnan(cb.lb) ? -INFINITY : cb.lb;
+            need = cb.some && !(lb > funkey(sh.bhi[slot]));
+          }
+          queue_exact(d, sh, need, 0, 3, slot, j, lb, lane);
+        } else {
+          int jj[2], kk[2], sl[2];
+          bool in[2];
+          CandBound cb[2];
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            const int i = ib + 32 * h + lane;
+            in[h] = i < tri0 + ntri;
+            const uint32_t it = in[h] ? sh.tri[i - tri0] : 0u;
+            jj[h] = (int)(it & 0xffffu);
+            kk[h] = (int)(it >> 16);
+            sl[h] = sh.cs[jj[h]];
+          }
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            float g[7];
+            screen_record(d, sh, jj[h], g);
+            const float tk = re_pow2f((int)g[6]);
+            const int k = kk[h], j = jj[h];
+            const float g12 = k == 0 ? g[3] : (k == 1 ? g[1] : g[0]);
+            const float g13 = k == 1 ? g[5] : g[4];
+            const float g23 = k == 0 ? g[5] : g[2];
+            const float pa = k == 1 ? sh.pf[j][1] : sh.pf[j][0];
+            const float pb = k == 0 ? sh.pf[j][1] : sh.pf[j][2];
+            cb[h] = tri_screen_bf(re_scale(re_in(g12), tk), re_scale(re_in(g13), tk), re_scale(re_in(g23), tk),
+                                  re_in(pa), re_in(pb));
+            if (exact_all) { cb[h].some = CAND_SOME; cb[h].lb = NAN; cb[h].ub = INFINITY; }
+          }
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            bool need = false;
+            float lb = 0.f;
+            if (in[h]) {
+              if (!exact_all && cb[h].some && cb[h].ub < INFINITY) atomicMin(&sh.bhi[sl[h]], fkey(cb[h].ub));
+              lb = isnan(cb[h].lb) ? -INFINITY : cb[h].lb;
+              need = cb[h].some && !(lb > funkey(sh.bhi[sl[h]]));
+            }
+            queue_exact(d, sh, need, 1, kk[h], sl[h], jj[h], lb, lane);
+          }
         }
-        queue_exact(d, sh, need, qi, kind, slot, j, lb, lane);
       }
       // then the edges that can still be the minimum
       for (int jb = 0; jb < kept; jb += kThreads) {
