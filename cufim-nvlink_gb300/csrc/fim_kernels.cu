@@ -431,7 +431,7 @@ constexpr int kTetCap = kCornerCap; // tet screens per batch: never full
 constexpr int kQcap = 768;          // exact solves queued per kind and batch (more run on the spot)
 // Phase D runs the queued tets on at most kDagWarps warps, one group of
 // kDagLanes lanes per tet (scratch: kDagGroups * kDagSlots doubles).
-constexpr int kDagWarps = 7;
+constexpr int kDagWarps = 10;
 constexpr int kDagGroups = kDagWarps * 32 / kDagLanes;
 
 // Order-preserving map of floats to unsigned integers (for atomicMin).
