@@ -424,8 +424,8 @@ __device__ __forceinline__ double dunkey(unsigned long long k)
 // FP64 pipe for 64 cycles whatever its active lanes, so two blocks per SM
 // would stack their FP64 warps on the same sub-partitions).
 constexpr int kThreads = kSolveThreads;  // threads per block of the solve kernel
-constexpr int kSlots = 128;         // vertices per batch (at most)
-constexpr int kCornerCap = 2560;    // corners per batch
+constexpr int kSlots = 160;         // vertices per batch (at most)
+constexpr int kCornerCap = 3072;    // corners per batch
 constexpr int kTriCap = kCornerCap * 6 / 5;  // triangle screens per batch (more are screened on the spot)
 constexpr int kTetCap = kCornerCap; // tet screens per batch: never full
 constexpr int kQcap = 768;          // exact solves queued per kind and batch (more run on the spot)
@@ -448,7 +448,9 @@ __device__ __forceinline__ float funkey(unsigned int k)
 // Shared memory of one batch of vertex updates.  Phase A loads everything a
 // corner's screens and decisions need once; the later phases read it from
 // here and go to global memory only for the FP64 operands of the solves
-// that survive the screens.
+// that survive the screens (and their vertex ids, from the corner record
+// phase A has read: not keeping 12 bytes of ids per corner here makes room
+// for 3072 corners a batch).
 struct BatchSh {
   int32_t vtx[kSlots];
   int32_t cnt[kSlots];              // corners of each vertex
@@ -458,7 +460,6 @@ struct BatchSh {
   unsigned long long res[kSlots];   // dkey of the running minimum (exact values)
   unsigned int bhi[kSlots];         // fkey of a float upper bound of the new time
   // per corner of the batch
-  int32_t nb[kCornerCap][3];        // the other three vertices
   union {
     struct {
       float pf[kCornerCap][3];      // their float times
@@ -482,12 +483,16 @@ struct BatchSh {
 static_assert(sizeof(double) * kDagGroups * kDagSlots <= sizeof(float) * kCornerCap * 6,
               "the tet prefix scratch must fit in the arrays it overlays");
 
-// Queue item: slot (7 bits) | kind (2 bits) | corner index in the batch (23 bits).
+// Queue item: slot (8 bits) | kind (2 bits) | corner index in the batch (22 bits).
 // kind: triangle pair 0..2 or 3 (tet) in queues 0 and 1, edge 0..2 in queue 2.
+static_assert(kSlots <= 256 && kCornerCap <= (1 << 22), "queue item fields");
 __device__ __forceinline__ uint32_t make_item(int slot, int kind, int j)
 {
-  return (uint32_t)slot | ((uint32_t)kind << 7) | ((uint32_t)j << 9);
+  return (uint32_t)slot | ((uint32_t)kind << 8) | ((uint32_t)j << 10);
 }
+__device__ __forceinline__ int item_slot(uint32_t it) { return (int)(it & 255u); }
+__device__ __forceinline__ int item_kind(uint32_t it) { return (int)((it >> 8) & 3u); }
+__device__ __forceinline__ int item_corner(uint32_t it) { return (int)(it >> 10); }
 
 // Appends one item per lane with `need` to a list in shared memory
 // (warp-ballot compaction).  Returns the item's position, or -1.
@@ -525,7 +530,7 @@ __device__ __forceinline__ double exact_solve(const FimDev &d, int64_t c, int ki
 // branch, for the warps that run only triangle solves).
 __device__ __forceinline__ double exact_tri(const FimDev &d, int64_t c, int kind, const int32_t *nb)
 {
-  const double pa = __ldcg(d.phi + nb[kind == 1 ? 1 : 0]), pb = __ldcg(d.phi + nb[kind == 0 ? 1 : 2]);
+  const double pa = __ldcg(d.phi + (kind == 1 ? nb[1] : nb[0])), pb = __ldcg(d.phi + (kind == 0 ? nb[1] : nb[2]));
   const double2 *gp = reinterpret_cast<const double2 *>(d.cgeo + kCgeoStride * c);
   const double2 t0 = __ldg(gp), t1 = __ldg(gp + 1), t2 = __ldg(gp + 2);
   const double e12 = kind == 0 ? t1.y : (kind == 1 ? t0.y : t0.x);
@@ -544,12 +549,24 @@ __device__ __forceinline__ double exact_edge(const FimDev &d, int64_t c, int i, 
   return __ldcg(d.phi + nbi) + sqrt(__ldg(d.cgeo + kCgeoStride * c + edge_slot(i)));
 }
 
+// The other three vertices of corner c (from its first-read record, which
+// phase A has just read: a cache hit).
+__device__ __forceinline__ void corner_nb(const FimDev &d, int64_t c, int32_t *nb)
+{
+  const uint4 id = __ldg(d.crec + kCrecWords * c);
+  nb[0] = (int32_t)id.x; nb[1] = (int32_t)id.y; nb[2] = (int32_t)id.z;
+}
+// nb[i] by selects (a runtime index would put nb in local memory)
+__device__ __forceinline__ int32_t pick3(const int32_t *nb, int i) { return i == 0 ? nb[0] : (i == 1 ? nb[1] : nb[2]); }
+
 // Evaluates queued item `it` (queue qi) in FP64 and folds it into the minimum.
 __device__ __forceinline__ void run_item(const FimDev &d, BatchSh &sh, int qi, uint32_t it)
 {
-  const int slot = it & 127, kind = (it >> 7) & 3, j = (int)(it >> 9);
+  const int slot = item_slot(it), kind = item_kind(it), j = item_corner(it);
   const int64_t c = sh.c0[slot] + (j - sh.cp[slot]);
-  const double val = qi == 2 ? exact_edge(d, c, kind, sh.nb[j][kind]) : exact_solve(d, c, kind, sh.nb[j]);
+  int32_t nb[3];
+  corner_nb(d, c, nb);
+  const double val = qi == 2 ? exact_edge(d, c, kind, pick3(nb, kind)) : exact_solve(d, c, kind, nb);
   if (val < FIM_INF) atomicMin(&sh.res[slot], dkey(val));
 }
 
@@ -684,9 +701,9 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
     const int total = sh.cp[nslot];     // may exceed kCornerCap for a single huge vertex
     const int kept = min(total, kCornerCap);
 
-    // A: load, validity, float edge bounds.  Pass 1 copies every corner's
-    // neighbour ids and float screen record to shared memory, pass 2 loads
-    // the neighbours' states and float times; within a pass the loads of a
+    // A: load, validity, float edge bounds.  Pass 1 loads every corner's
+    // first-read record (ids, float lengths, fp16 bounds), pass 2 the
+    // neighbours' states and float times; within a pass the loads of a
     // thread's corners are independent, so they are all in flight together.
     for (int jb = 0; jb < kept; jb += kPer * kThreads) {
       // all of a thread's record loads first, then the neighbour loads that
@@ -732,7 +749,6 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
         if (j < kept) {
           sh.hb[j][0] = h0[r].w;
           sh.hb[j][1] = h1[r].w;
-          sh.nb[j][0] = (int32_t)h0[r].x; sh.nb[j][1] = (int32_t)h0[r].y; sh.nb[j][2] = (int32_t)h0[r].z;
           sh.sf[j][0] = __uint_as_float(h1[r].x); sh.sf[j][1] = __uint_as_float(h1[r].y);
           sh.sf[j][2] = __uint_as_float(h1[r].z);
           sh.cs[j] = (uint8_t)slot[r];
@@ -751,7 +767,11 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
           if (ok) {
             if (re_lo(P) > lower_hi) ok = true;
             else if (re_hi(P) <= lower_lo) ok = false;
-            else ok = __ldcg(d.phi + sh.nb[j][i]) > lower;
+            else {  // rare: the FP64 time decides
+              int32_t nb[3];
+              corner_nb(d, sh.c0[slot[r]] + (j - sh.cp[slot[r]]), nb);
+              ok = __ldcg(d.phi + pick3(nb, i)) > lower;
+            }
           }
           if (ok) {
             m |= 1u << i;
@@ -965,14 +985,16 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
           bool run = false;
           if (pos < ntet) {
             const uint32_t it = sh.q[0][pos];
-            slot = it & 127;
+            slot = item_slot(it);
             run = !(sh.qlb[0][pos] > funkey(sh.bhi[slot]));  // else overtaken by a later bound
             if (run) {
-              const int jj = (int)(it >> 9);
+              const int jj = item_corner(it);
               const int64_t c = sh.c0[slot] + (jj - sh.cp[slot]);
               // leaves: e13 e23 e34 e12 e14 e24 p1 p2 (lanes 0..7), p3, 0.5 2.0 1.0 -0.0
-              S[gl] = gl < 6 ? __ldg(d.cgeo + kCgeoStride * c + gl) : __ldcg(d.phi + sh.nb[jj][gl - 6]);
-              if (gl == 0) S[kDagLeafP1 + 2] = __ldcg(d.phi + sh.nb[jj][2]);
+              int32_t nb[3];
+              corner_nb(d, c, nb);
+              S[gl] = gl < 6 ? __ldg(d.cgeo + kCgeoStride * c + gl) : __ldcg(d.phi + (gl == 6 ? nb[0] : nb[1]));
+              if (gl == 0) S[kDagLeafP1 + 2] = __ldcg(d.phi + nb[2]);
               else if (gl <= 4) S[kDagLeafConst + gl - 1] = gl == 1 ? 0.5 : (gl == 2 ? 2.0 : (gl == 3 ? 1.0 : -0.0));
             }
           }
@@ -997,10 +1019,12 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
         else if (j >= edge0) { qi = 2; pos = j - edge0; }
         else continue;
         const uint32_t it = sh.q[qi][pos];
-        if (sh.qlb[qi][pos] > funkey(sh.bhi[it & 127])) continue;  // overtaken by a later bound
-        const int slot = it & 127, kind = (it >> 7) & 3, jj = (int)(it >> 9);
+        if (sh.qlb[qi][pos] > funkey(sh.bhi[item_slot(it)])) continue;  // overtaken by a later bound
+        const int slot = item_slot(it), kind = item_kind(it), jj = item_corner(it);
         const int64_t c = sh.c0[slot] + (jj - sh.cp[slot]);
-        const double val = qi == 2 ? exact_edge(d, c, kind, sh.nb[jj][kind]) : exact_tri(d, c, kind, sh.nb[jj]);
+        int32_t nb[3];
+        corner_nb(d, c, nb);
+        const double val = qi == 2 ? exact_edge(d, c, kind, pick3(nb, kind)) : exact_tri(d, c, kind, nb);
         if (val < FIM_INF) atomicMin(&sh.res[slot], dkey(val));
         if (qi < 2) ++n_exact;
       }
