@@ -399,12 +399,6 @@ __device__ bool grid_sync(FimCtl *ctl, uint32_t nblocks, uint64_t timeout_ns, in
 // ---------------------------------------------------------------------------
 // persistent solve
 
-struct WarpCtx {
-  int lane;
-  int64_t gwarp;
-  int64_t nwarps;
-};
-
 // Order-preserving map of doubles to unsigned integers, so that the minimum
 // of a vertex's candidates can be formed with integer atomicMin.
 __device__ __forceinline__ unsigned long long dkey(double x)
@@ -424,6 +418,8 @@ __device__ __forceinline__ double dunkey(unsigned long long k)
 // FP64 pipe for 64 cycles whatever its active lanes, so two blocks per SM
 // would stack their FP64 warps on the same sub-partitions).
 constexpr int kThreads = kSolveThreads;  // threads per block of the solve kernel
+constexpr int kMarkLanes = 16;           // threads per frozen vertex in the neighbour marking
+static_assert(kThreads % kMarkLanes == 0, "marking groups must tile the grid");
 constexpr int kSlots = 160;         // vertices per batch (at most)
 constexpr int kCornerCap = 3072;    // corners per batch
 constexpr int kTriCap = kCornerCap * 6 / 5;  // triangle screens per batch (more are screened on the spot)
@@ -1061,10 +1057,6 @@ __global__ void __launch_bounds__(kThreads, 1) fim_solve_kernel(FimDev d, FimPar
   const uint32_t nblocks = gridDim.x;
   const int64_t gtid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
-  WarpCtx w;
-  w.lane = threadIdx.x & 31;
-  w.gwarp = gtid >> 5;
-  w.nwarps = nthreads >> 5;
   int64_t my_evals = 0, my_updates = 0, my_exact = 0;
   int where = 0;
   extern __shared__ __align__(16) unsigned char fim_smem[];
@@ -1153,16 +1145,19 @@ __global__ void __launch_bounds__(kThreads, 1) fim_solve_kernel(FimDev d, FimPar
       if (!grid_sync(ctl, nblocks, p.timeout_ns, ++where)) return;
 
       // P2 -- apply the narrow times; mark downwind neighbours of the
-      // vertices frozen now (cuda_fim.cu:2172-2205)
-      for (int64_t i = gtid; i < nn; i += nthreads) {
+      // vertices frozen now (cuda_fim.cu:2172-2205).  The two are
+      // independent: the marking runs on groups of kMarkLanes threads from
+      // the bottom of the grid, the apply on threads from the top, so that
+      // their dependent load chains overlap.
+      for (int64_t i = nthreads - 1 - gtid; i < nn; i += nthreads) {
         const int32_t v = lst[i];
         set_phi(d, v, __ldcg(d.phi2 + v));
       }
       const int32_t nf = ld_volatile_i32(&ctl->n_frozen[s]);
-      for (int64_t i = w.gwarp; i < nf; i += w.nwarps) {
+      for (int64_t i = gtid / kMarkLanes; i < nf; i += nthreads / kMarkLanes) {
         const int32_t n = d.lfrozen[i];
         const double pn = __ldcg(d.phi2 + n);
-        for (int64_t k = d.nptr[n] + w.lane; k < d.nptr[n + 1]; k += 32) {
+        for (int64_t k = d.nptr[n] + gtid % kMarkLanes; k < d.nptr[n + 1]; k += kMarkLanes) {
           const int32_t v = __ldg(d.nbr + k);
           if (__ldcg(d.st + v) != ST_NARROW && pn < __ldcg(d.phi2 + v)) {
             if (atomicExch(d.flag + v, stamp) != stamp) {
@@ -1181,23 +1176,27 @@ __global__ void __launch_bounds__(kThreads, 1) fim_solve_kernel(FimDev d, FimPar
       my_updates += (gtid == 0) ? nm : 0;
       if (!grid_sync(ctl, nblocks, p.timeout_ns, ++where)) return;
 
-      // P4 -- apply, update neighbour states, next narrow list (cuda_fim.cu:2291-2317)
-      for (int64_t i = gtid; i < nm; i += nthreads) {
-        const int32_t v = d.lmarked[i];
-        set_phi(d, v, __ldcg(d.phi2 + v));
-        uint8_t sv = __ldcg(d.dec + i);
-        if (sv == ST_NARROW) {
-          if (__ldcg(d.tst + v) == ST_FROZEN) sv = ST_FROZEN;
-          else lnext[atomicAdd(&ctl->n_narrow[s1], 1)] = v;
-        }
-        d.st[v] = sv;
-      }
-      for (int64_t i = gtid; i < nn; i += nthreads) {
-        const int32_t v = lst[i];
-        if (__ldcg(d.flag + v) == stamp) continue;  // re-solved above
-        if (__ldcg(d.st + v) == ST_NARROW) {
-          if (__ldcg(d.tst + v) == ST_FROZEN) d.st[v] = ST_FROZEN;
-          else lnext[atomicAdd(&ctl->n_narrow[s1], 1)] = v;
+      // P4 -- apply, update neighbour states, next narrow list (cuda_fim.cu:2291-2317):
+      // the re-solved neighbours, then (one index space, so that both run
+      // at once: they touch disjoint vertices) the narrow vertices that
+      // were not re-solved
+      for (int64_t i = gtid; i < (int64_t)nm + nn; i += nthreads) {
+        if (i < nm) {
+          const int32_t v = d.lmarked[i];
+          set_phi(d, v, __ldcg(d.phi2 + v));
+          uint8_t sv = __ldcg(d.dec + i);
+          if (sv == ST_NARROW) {
+            if (__ldcg(d.tst + v) == ST_FROZEN) sv = ST_FROZEN;
+            else lnext[atomicAdd(&ctl->n_narrow[s1], 1)] = v;
+          }
+          d.st[v] = sv;
+        } else {
+          const int32_t v = lst[i - nm];
+          if (__ldcg(d.flag + v) == stamp) continue;  // re-solved above
+          if (__ldcg(d.st + v) == ST_NARROW) {
+            if (__ldcg(d.tst + v) == ST_FROZEN) d.st[v] = ST_FROZEN;
+            else lnext[atomicAdd(&ctl->n_narrow[s1], 1)] = v;
+          }
         }
       }
       ++it;
