@@ -1158,10 +1158,14 @@ __global__ void __launch_bounds__(kThreads, 1) fim_solve_kernel(FimDev d, FimPar
         const int32_t n = d.lfrozen[i];
         const double pn = __ldcg(d.phi2 + n);
         for (int64_t k = d.nptr[n] + gtid % kMarkLanes; k < d.nptr[n + 1]; k += kMarkLanes) {
+          // both loads at once; st[v] changes only after the exchange below,
+          // by its winner, so sv is still v's state there
           const int32_t v = __ldg(d.nbr + k);
-          if (__ldcg(d.st + v) != ST_NARROW && pn < __ldcg(d.phi2 + v)) {
+          const uint8_t sv = __ldcg(d.st + v);
+          const double pv = __ldcg(d.phi2 + v);
+          if (sv != ST_NARROW && pn < pv) {
             if (atomicExch(d.flag + v, stamp) != stamp) {
-              d.tst[v] = __ldcg(d.st + v);
+              d.tst[v] = sv;
               d.st[v] = ST_NEIG;
               d.lmarked[atomicAdd(&ctl->n_marked[s], 1)] = v;
             }
@@ -1183,18 +1187,22 @@ __global__ void __launch_bounds__(kThreads, 1) fim_solve_kernel(FimDev d, FimPar
       for (int64_t i = gtid; i < (int64_t)nm + nn; i += nthreads) {
         if (i < nm) {
           const int32_t v = d.lmarked[i];
-          set_phi(d, v, __ldcg(d.phi2 + v));
           uint8_t sv = __ldcg(d.dec + i);
+          const uint8_t tv = __ldcg(d.tst + v);
+          set_phi(d, v, __ldcg(d.phi2 + v));
           if (sv == ST_NARROW) {
-            if (__ldcg(d.tst + v) == ST_FROZEN) sv = ST_FROZEN;
+            if (tv == ST_FROZEN) sv = ST_FROZEN;
             else lnext[atomicAdd(&ctl->n_narrow[s1], 1)] = v;
           }
           d.st[v] = sv;
         } else {
+          // the three loads at once (a re-solved vertex's are not used)
           const int32_t v = lst[i - nm];
-          if (__ldcg(d.flag + v) == stamp) continue;  // re-solved above
-          if (__ldcg(d.st + v) == ST_NARROW) {
-            if (__ldcg(d.tst + v) == ST_FROZEN) d.st[v] = ST_FROZEN;
+          const int32_t fv = __ldcg(d.flag + v);
+          const uint8_t sv = __ldcg(d.st + v), tv = __ldcg(d.tst + v);
+          if (fv == stamp) continue;  // re-solved above
+          if (sv == ST_NARROW) {
+            if (tv == ST_FROZEN) d.st[v] = ST_FROZEN;
             else lnext[atomicAdd(&ctl->n_narrow[s1], 1)] = v;
           }
         }
