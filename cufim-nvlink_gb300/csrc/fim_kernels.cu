@@ -968,14 +968,18 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
     {
       const int ntet = min(sh.nq[0], kQcap), ntri = min(sh.nq[1], kQcap), nedge = min(sh.nq[2], kQcap);
       // tets: one group of kDagLanes lanes per tet runs the prefix
-      // (tet_dag_prefix), then the group's first two lanes one root each;
-      // groups of kDagWarps warps at most, warp-uniform loop
+      // (tet_dag_prefix); then the roots, two per tet, on consecutive
+      // threads from thread 0, so that they fill as few warps as possible
+      // (an FP64 warp instruction costs the same for any number of active
+      // lanes); groups of kDagWarps warps at most, a loop uniform over the
+      // tet warps, which meet at named barrier 1 between prefix and roots
       const int tet_warps = min(kDagWarps, (ntet * kDagLanes + 31) / 32);
       const int tri0 = 32 * tet_warps;
       if (tid < tri0) {
         const int grp = tid / kDagLanes, gl = tid % kDagLanes;
         double *S = sh.dag[grp];
-        for (int base = 0; base < ntet; base += tri0 / kDagLanes) {
+        const int ngrp = tri0 / kDagLanes;
+        for (int base = 0; base < ntet; base += ngrp) {
           const int pos = base + grp;
           int slot = 0;
           bool run = false;
@@ -996,15 +1000,18 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
           }
           __syncwarp();
           tet_dag_prefix(S, gl);
-          double val = FIM_INF;
-          if (run && gl < 2) val = tet_root_tail(S, gl == 1);
-          const double other = __shfl_xor_sync(FULL_MASK, val, 1);
-          if (run && gl == 0) {
-            const double v = fmin(val, other);
-            ++n_exact;
-            if (v < FIM_INF) atomicMin(&sh.res[slot], dkey(v));
+          asm volatile("bar.sync 1, %0;" ::"r"(tri0) : "memory");
+          const int rpos = base + (tid >> 1);  // root (tid & 1) of tet rpos
+          if (tid < 2 * ngrp && rpos < ntet) {
+            const uint32_t it = sh.q[0][rpos];
+            const int rslot = item_slot(it);
+            if (!(sh.qlb[0][rpos] > funkey(sh.bhi[rslot]))) {
+              const double v = tet_root_tail(sh.dag[tid >> 1], (tid & 1) != 0);
+              if ((tid & 1) == 0) ++n_exact;
+              if (v < FIM_INF) atomicMin(&sh.res[rslot], dkey(v));
+            }
           }
-          __syncwarp();  // the next pass overwrites S
+          asm volatile("bar.sync 1, %0;" ::"r"(tri0) : "memory");  // the next pass overwrites the scratch
         }
       }
       const int edge0 = tri0 + ((ntri + 31) & ~31);
