@@ -96,6 +96,16 @@ __device__ __forceinline__ bool din01(double x)
 {
   return (unsigned long long)__double_as_longlong(x) - 1ull < 0x3fefffffffffffffull;
 }
+// 0 < x < inf (false for NaN)
+__device__ __forceinline__ bool dpos_finite(double x)
+{
+  return (unsigned long long)__double_as_longlong(x) - 1ull < 0x7fefffffffffffffull;
+}
+// x finite (not inf, not NaN)
+__device__ __forceinline__ bool dfinite(double x)
+{
+  return ((unsigned long long)__double_as_longlong(x) & 0x7ff0000000000000ull) != 0x7ff0000000000000ull;
+}
 // x < 0 (false for zeros and NaN)
 __device__ __forceinline__ bool dlt0(double x)
 {
@@ -268,8 +278,9 @@ __global__ void fim_metric_kernel(const int32_t *__restrict__ tslots, const int6
     const double f0 = fib[3 * e + 0], f1 = fib[3 * e + 1], f2 = fib[3 * e + 2];
     // the input check of fim_set_conduction: positive finite speeds, finite
     // fibre; the first offending tet is reported
-    if (!(cf[e] > 0.0 && ct[e] > 0.0 && isfinite(cf[e]) && isfinite(ct[e]) && isfinite(f0) && isfinite(f1) &&
-          isfinite(f2)))
+    // (sign and exponent tests on the integer pipes: the FP64 pipe is this
+    // kernel's bound)
+    if (!(dpos_finite(cf[e]) && dpos_finite(ct[e]) && dfinite(f0) && dfinite(f1) && dfinite(f2)))
       atomicMin(bad, (unsigned long long)e);
     const double fa = f0*f0, fb = f0*f1, fc = f0*f2, fd = f1*f1, fe = f1*f2, ff = f2*f2;
     const double vf = 1. / cf[e] / cf[e], vs = 1. / ct[e] / ct[e];
@@ -292,14 +303,18 @@ __global__ void fim_metric_kernel(const int32_t *__restrict__ tslots, const int6
       const double ez = xyz[3 * (int64_t)va[k] + 2] - xyz[3 * (int64_t)vb[k] + 2];
       g[k] = (M0*ex + M1*ey + M2*ez)*ex + (M1*ex + M3*ey + M4*ez)*ey + (M2*ex + M4*ey + M5*ez)*ez;
     }
-    // scale 2^-k (k even) of the float screen record: edge norms O(1)
-    double gmax = g[0];
+    // scale 2^-k (k even) of the float screen record: edge norms O(1).  The
+    // largest norm by its bit pattern (the order of non-negative doubles;
+    // a negative or NaN norm only turns the scaling off), its binary
+    // exponent from the exponent field (a subnormal maximum is out of range
+    // either way), all on the integer pipes
+    long long gbits = __double_as_longlong(g[0]);
 #pragma unroll
-    for (int kk = 1; kk < 6; ++kk) gmax = fmax(gmax, g[kk]);
-    int ex = 0;
-    frexp(gmax, &ex);
+    for (int kk = 1; kk < 6; ++kk) gbits = max(gbits, __double_as_longlong(g[kk]));
+    const double gmax = __longlong_as_double(gbits);
+    const int ex = (int)((gbits >> 52) & 0x7ff) - 1022;  // frexp's exponent for a normal gmax
     int ks = ex & ~1;
-    const bool ok = isfinite(gmax) && gmax > 0.0 && ks <= 50 && ks >= -50;
+    const bool ok = dpos_finite(gmax) && ks <= 50 && ks >= -50;
     if (!ok) ks = 0;
     const float tk = ldexpf(1.f, ks / 2);
     // FP32 copies of the edge norms (scaled) and of the three edge lengths
