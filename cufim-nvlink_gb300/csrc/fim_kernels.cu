@@ -888,21 +888,39 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
     // warp is free -- tets first (32 per chunk, one per lane), then triangles
     // from the next chunk boundary (64 per chunk: each lane screens two with
     // the branch-free tri_screen_bf, so that the two chains interleave), so
-    // that every chunk holds one kind; a solve whose lower bound does not
-    // exceed the current bhi is queued at once (bhi only decreases: phase D
-    // rechecks against the final bound)
+    // that every chunk holds one kind, and last the edges of 32 corners per
+    // chunk; a solve whose lower bound does not exceed the current bhi is
+    // queued at once (bhi only decreases: phase D rechecks against the final
+    // bound)
     {
       const int ntet = min(sh.ntet, kTetCap), ntri = min(sh.ntri, kTriCap);
       const int tri0 = (ntet + 31) & ~31;
+      const int edge_c0 = tri0 + ((ntri + 63) / 64) * 32;  // claim index of the first edge chunk
+      const int nclaim = edge_c0 + ((kept + 31) & ~31);
       for (;;) {
-        // tet chunks of 32 items, then triangle chunks of 64 (two per lane)
-        int ib = 0;
-        if (lane == 0) {
-          ib = atomicAdd(&sh.next_item, 32);
-          if (ib >= tri0) ib = tri0 + 2 * (ib - tri0);  // 32 claimed in the triangle range stand for 64
+        // claims of 32: tet chunks, then triangle chunks of 64 (two per
+        // lane), then edge chunks of 32 corners
+        int cl = 0;
+        if (lane == 0) cl = atomicAdd(&sh.next_item, 32);
+        cl = __shfl_sync(FULL_MASK, cl, 0);
+        if (cl >= nclaim) break;
+        if (cl >= edge_c0) {
+          // the edges that can still be the minimum
+          const int j = cl - edge_c0 + lane;
+          const bool in = j < kept;
+          int slot = 0;
+          uint32_t m = 0;
+          float bhi = 0.f;
+          if (in) { slot = sh.cs[j]; m = sh.vm[j]; bhi = funkey(sh.bhi[slot]); }
+#pragma unroll
+          for (int i = 0; i < 3; ++i) {
+            const float le = in ? re_lo(re_in(sh.pf[j][i]) + re_len(sh.sf[j][i])) : 0.f;
+            const bool need = in && ((m >> i) & 1u) && !(le > bhi);
+            queue_exact(d, sh, need, 2, i, slot, j, le, lane);
+          }
+          continue;
         }
-        ib = __shfl_sync(FULL_MASK, ib, 0);
-        if (ib >= tri0 + ntri) break;
+        const int ib = cl < tri0 ? cl : tri0 + 2 * (cl - tri0);  // 32 claimed in the triangle range stand for 64
         if (ib < tri0) {
           const int i = ib + lane;
           bool need = false;
@@ -958,21 +976,6 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
             }
             queue_exact(d, sh, need, 1, kk[h], sl[h], jj[h], lb, lane);
           }
-        }
-      }
-      // then the edges that can still be the minimum
-      for (int jb = 0; jb < kept; jb += kThreads) {
-        const int j = jb + tid;
-        const bool in = j < kept;
-        int slot = 0;
-        uint32_t m = 0;
-        float bhi = 0.f;
-        if (in) { slot = sh.cs[j]; m = sh.vm[j]; bhi = funkey(sh.bhi[slot]); }
-#pragma unroll
-        for (int i = 0; i < 3; ++i) {
-          const float le = in ? re_lo(re_in(sh.pf[j][i]) + re_len(sh.sf[j][i])) : 0.f;
-          const bool need = in && ((m >> i) & 1u) && !(le > bhi);
-          queue_exact(d, sh, need, 2, i, slot, j, le, lane);
         }
       }
     }
