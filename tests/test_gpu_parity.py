@@ -336,10 +336,11 @@ def _pincushion(n_sphere, seed):
                 seed_v=np.array([1, 2, 3]), seed_t=np.array([0.0, 0.5, 1.0]))
 
 
-@pytest.mark.parametrize("n_sphere", [1400, 3000])
+@pytest.mark.parametrize("n_sphere", [1400, 1600, 3000])
 def test_high_valence_vertex_bit_exact(F, O, n_sphere):
-    """A vertex with more corners than one batch holds (2,796 and 5,996
-    tets around it) goes through the all-FP64 path for the excess; the
+    """A vertex with 2,796 tets around it fills most of a batch (3,072
+    corners) on its own; one with 3,196 or 5,996 has more corners than a
+    batch holds and goes through the all-FP64 path for the excess; the
     result is still the oracle's, bit for bit, screened or not."""
     pytest.importorskip("scipy")
     c = _pincushion(n_sphere, 3)
