@@ -273,17 +273,41 @@ __global__ void fim_metric_kernel(const int32_t *__restrict__ tslots, const int6
                                   int64_t e0, int64_t e1, double *__restrict__ cgeo, float *__restrict__ cgf,
                                   uint4 *__restrict__ crec, unsigned long long *__restrict__ bad)
 {
-  for (int64_t e = e0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < e1;
-       e += (int64_t)gridDim.x * blockDim.x) {
+  // The speed terms 1/cf/cf and 1/ct/ct cost four FP64 divisions, and an
+  // FP64 warp instruction costs the same for one active lane as for 32.  So
+  // thread 0 of the block evaluates them for its own tet, and every warp
+  // whose tets all have the same speeds (bit for bit) takes that result
+  // instead of dividing: with piecewise-constant conduction most warps do.
+  __shared__ double s_sp[4];  // thread 0's cf, ct and their 1/cf/cf, 1/ct/ct
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t eb = e0 + blockIdx.x * (int64_t)blockDim.x; eb < e1; eb += stride) {  // block-uniform
+    const int64_t e = eb + threadIdx.x;
+    const bool in = e < e1;
+    const double cfe = in ? cf[e] : 0.0, cte = in ? ct[e] : 0.0;
+    if (threadIdx.x == 0) {  // eb < e1: thread 0 is in range
+      s_sp[0] = cfe; s_sp[1] = cte;
+      s_sp[2] = 1. / cfe / cfe; s_sp[3] = 1. / cte / cte;
+    }
+    __syncthreads();
+    const bool same = !in || (__double_as_longlong(cfe) == __double_as_longlong(s_sp[0]) &&
+                              __double_as_longlong(cte) == __double_as_longlong(s_sp[1]));
+    double vf, vs;
+    if (__all_sync(0xffffffffu, same)) {
+      vf = s_sp[2]; vs = s_sp[3];
+    } else {
+      vf = 1. / cfe / cfe; vs = 1. / cte / cte;
+    }
+    __syncthreads();  // s_sp is rewritten by the next round
+    if (!in) continue;
     const double f0 = fib[3 * e + 0], f1 = fib[3 * e + 1], f2 = fib[3 * e + 2];
     // the input check of fim_set_conduction: positive finite speeds, finite
     // fibre; the first offending tet is reported
     // (sign and exponent tests on the integer pipes: the FP64 pipe is this
     // kernel's bound)
-    if (!(dpos_finite(cf[e]) && dpos_finite(ct[e]) && dfinite(f0) && dfinite(f1) && dfinite(f2)))
+    if (!(dpos_finite(cfe) && dpos_finite(cte) && dfinite(f0) && dfinite(f1) && dfinite(f2)))
       atomicMin(bad, (unsigned long long)e);
+    // compute_velocity_tensor_f3 (types.h:173-188)
     const double fa = f0*f0, fb = f0*f1, fc = f0*f2, fd = f1*f1, fe = f1*f2, ff = f2*f2;
-    const double vf = 1. / cf[e] / cf[e], vs = 1. / ct[e] / ct[e];
     const double M0 = vf*fa + vs*(1. - fa);
     const double M1 = (vf - vs)*fb;
     const double M2 = (vf - vs)*fc;
