@@ -595,7 +595,7 @@ __device__ __forceinline__ void corner_nb(const FimDev &d, int64_t c, int32_t *n
 __device__ __forceinline__ int32_t pick3(const int32_t *nb, int i) { return i == 0 ? nb[0] : (i == 1 ? nb[1] : nb[2]); }
 
 // Evaluates queued item `it` (queue qi) in FP64 and folds it into the minimum.
-__device__ __forceinline__ void run_item(const FimDev &d, BatchSh &sh, int qi, uint32_t it)
+__device__ __noinline__ void run_item(const FimDev &d, BatchSh &sh, int qi, uint32_t it)
 {
   const int slot = item_slot(it), kind = item_kind(it), j = item_corner(it);
   const int64_t c = sh.c0[slot] + (j - sh.cp[slot]);
@@ -651,6 +651,17 @@ __device__ __forceinline__ CandBound tet_screen_sm(const FimDev &d, const BatchS
   screen_record(d, sh, j, g);
   const Re gs[6] = {re_in(g[0]), re_in(g[1]), re_in(g[2]), re_in(g[3]), re_in(g[4]), re_in(g[5])};
   return tet_screen(gs, re_in(sh.pf[j][0]), re_in(sh.pf[j][1]), re_in(sh.pf[j][2]), (int)g[6]);
+}
+
+// A triangle pair that finds the screen list full: screened (and solved)
+// on the spot; out of line, since it is rare and large.
+__device__ __noinline__ void tri_list_full(const FimDev &d, BatchSh &sh, int j, int k, int slot, float bhi,
+                                           bool exact_all)
+{
+  CandBound cb;
+  if (exact_all) { cb.some = CAND_SOME; cb.lb = NAN; cb.ub = INFINITY; }
+  else cb = tri_screen_sm(d, sh, j, k);
+  if (cb.some && !(cb.lb > bhi)) run_item(d, sh, 1, make_item(slot, k, j));
 }
 
 // Writes a time and its float copy.
@@ -893,10 +904,7 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
           if (p < kTriCap) {
             sh.tri[p] = (uint32_t)j | ((uint32_t)k << 16);
           } else {  // list full: screen here
-            CandBound cb;
-            if (exact_all) { cb.some = CAND_SOME; cb.lb = NAN; cb.ub = INFINITY; }
-            else cb = tri_screen_sm(d, sh, j, k);
-            if (cb.some && !(cb.lb > bhi)) run_item(d, sh, 1, make_item(slot, k, j));
+            tri_list_full(d, sh, j, k, slot, bhi, exact_all);
           }
         }
       }
