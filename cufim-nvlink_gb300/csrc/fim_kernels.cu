@@ -664,6 +664,36 @@ __device__ __noinline__ void tri_list_full(const FimDev &d, BatchSh &sh, int j, 
   if (cb.some && !(cb.lb > bhi)) run_item(d, sh, 1, make_item(slot, k, j));
 }
 
+// The corners of a batch beyond kCornerCap (only a batch of one vertex, in
+// slot 0, has them): every solve of them in FP64, the reference's validity
+// on the FP64 times.  Returns the corners with a valid neighbour.
+__device__ __noinline__ int64_t excess_corners(const FimDev &d, BatchSh &sh, int kept, int total, double lower)
+{
+  int64_t n_valid = 0;
+  for (int j = kept + (int)threadIdx.x; j < total; j += kThreads) {
+    const int slot = 0;
+    const int64_t c = sh.c0[slot] + (j - sh.cp[slot]);
+    const uint4 id = __ldg(d.crec + kCrecWords * c);
+    const int32_t nb[3] = {(int32_t)id.x, (int32_t)id.y, (int32_t)id.z};
+    uint32_t m = 0;
+    for (int i = 0; i < 3; ++i) {
+      const double p = __ldcg(d.phi + nb[i]);
+      if (__ldcg(d.st + nb[i]) >= ST_NARROW && p > lower) {
+        m |= 1u << i;
+        atomicMin(&sh.res[slot], dkey(p + sqrt(__ldg(d.cgeo + kCgeoStride * c + edge_slot(i)))));
+      }
+    }
+    if (m) ++n_valid;
+    for (int k = 0; k < 4; ++k) {
+      const bool use = k == 3 ? m == 7u : (((m >> (k == 1 ? 1 : 0)) & 1u) && ((m >> (k == 0 ? 1 : 2)) & 1u));
+      if (!use) continue;
+      const double val = exact_solve(d, c, k, nb);
+      if (val < FIM_INF) atomicMin(&sh.res[slot], dkey(val));
+    }
+  }
+  return n_valid;
+}
+
 // Writes a time and its float copy.
 __device__ __forceinline__ void set_phi(const FimDev &d, int64_t v, double x)
 {
@@ -832,27 +862,7 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
     }
     // corners beyond kCornerCap (a single vertex with very many corners):
     // every solve of them goes to FP64
-    for (int j = kept + tid; j < total; j += kThreads) {
-      const int slot = 0;  // only a batch of one vertex has such corners
-      const int64_t c = sh.c0[slot] + (j - sh.cp[slot]);
-      const uint4 id = __ldg(d.crec + kCrecWords * c);
-      const int32_t nb[3] = {(int32_t)id.x, (int32_t)id.y, (int32_t)id.z};
-      uint32_t m = 0;
-      for (int i = 0; i < 3; ++i) {
-        const double p = __ldcg(d.phi + nb[i]);
-        if (__ldcg(d.st + nb[i]) >= ST_NARROW && p > lower) {
-          m |= 1u << i;
-          atomicMin(&sh.res[slot], dkey(p + sqrt(__ldg(d.cgeo + kCgeoStride * c + edge_slot(i)))));
-        }
-      }
-      if (m) ++n_filtered;
-      for (int k = 0; k < 4; ++k) {
-        const bool use = k == 3 ? m == 7u : (((m >> (k == 1 ? 1 : 0)) & 1u) && ((m >> (k == 0 ? 1 : 2)) & 1u));
-        if (!use) continue;
-        const double val = exact_solve(d, c, k, nb);
-        if (val < FIM_INF) atomicMin(&sh.res[slot], dkey(val));
-      }
-    }
+    if (total > kept) n_filtered += excess_corners(d, sh, kept, total, lower);
     __syncthreads();
 
     // B: screen lists
