@@ -704,19 +704,23 @@ __device__ __forceinline__ void set_phi(const FimDev &d, int64_t v, double x)
 // One update phase over a vertex list.  Every block takes a contiguous part
 // of the list and processes it in batches of up to kSlots vertices / up to
 // kCornerCap corners, the corners of a batch spread over all threads:
-//  A -- load every corner once (neighbour ids, float screen record,
-//       neighbour states and float times), validity of the neighbours
-//       (state >= narrow and phi > phi_start - front_width, on the float
-//       copies when conclusive, else on the FP64 times), float edge bounds
-//       -> per-vertex upper bound bhi of the new time;
-//  B -- triangle and tet solves whose trivial bound min(neighbour times)
-//       <= bhi are appended to compacted screen lists (warp ballots);
-//  S -- the screens run over the lists with full warps (triangles and tets
-//       on separate warps); certain upper bounds tighten bhi;
-//       a solve whose lower bound does not exceed the current bhi is queued
-//       at once, and so are the edges that can still be the minimum;
+//  A -- load every corner's first-read record once (neighbour ids, float
+//       edge lengths, fp16 root-term bounds) and its neighbours' states and
+//       float times; validity of the neighbours (state >= narrow and
+//       phi > phi_start - front_width, on the float copies when conclusive,
+//       else on the FP64 times), float edge bounds -> per-vertex upper
+//       bound bhi of the new time;
+//  B -- triangle and tet solves whose lower bound min(neighbour times) +
+//       root-term bound does not exceed bhi are appended to compacted
+//       screen lists (warp ballots);
+//  S -- the FP32 screens run over the lists in chunks claimed by whichever
+//       warp is free (tets, then triangles, then the edge checks); certain
+//       upper bounds tighten bhi; a solve whose lower bound does not exceed
+//       the current bhi is queued at once, and so are the edges that can
+//       still be the minimum;
 //  D -- the queued solves whose lower bound does not exceed the final bhi run
-//       in FP64 (tets, triangles and edges each from a warp boundary);
+//       in FP64 (tet prefixes on 8-lane groups and their roots packed from
+//       thread 0; triangles and edges each from a warp boundary);
 //  E -- the reference's per-vertex decision on the exact minimum:
 //   mode 0 -- narrow vertices: window test (next), freeze test
 //             (cuda_fim.cu:2125-2163);
