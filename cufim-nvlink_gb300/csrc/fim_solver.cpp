@@ -577,9 +577,10 @@ extern "C" int fim_set_stimuli(fim_solver *s, int64_t n, const int64_t *vertices
                      (long long)vertices[i], (long long)s->nV);
     if (!std::isfinite(t0[i]))
       return set_err(s, FIM_ERR_INVALID_ARGUMENT, "fim_set_stimuli: start time %lld is not finite", (long long)i);
+    const double ti = t0[i] == 0.0 ? 0.0 : t0[i];  // -0.0 counts as +0.0
     auto it = first.find(vertices[i]);
-    if (it == first.end()) first.emplace(vertices[i], t0[i]);
-    else if (t0[i] < it->second) it->second = t0[i];
+    if (it == first.end()) first.emplace(vertices[i], ti);
+    else if (ti < it->second) it->second = ti;
   }
   // every copy of a stimulated vertex is seeded (update_events_gpu seeds
   // through the submeshes holding the vertex, cuda_fim.cu:1422-1487)
@@ -766,6 +767,7 @@ extern "C" int fim_solve_noalloc(fim_solver *s, int64_t n, const int64_t *vertic
   d.list[0] = sc.list[0]; d.list[1] = sc.list[1]; d.list[2] = sc.list[2];
   d.lfrozen = sc.lfrozen; d.lmarked = sc.lmarked; d.dec = sc.dec;
   d.seed_v = sc.seed_v; d.seed_t = sc.seed_t; d.nseed = (int32_t)entries;
+  d.phi_init = s->warm;  // the caller's own device array (fim_set_warm_start): nothing to allocate
   d.ctl = sc.ctl;
   FimParams p{};
   p.dt = s->opts.dt;

@@ -62,9 +62,12 @@ std::mutex g_setup_mu;
 unsigned char *g_base[kMaxDevices] = {};
 
 // Order-preserving key of a finite double (smaller time -> smaller key).
+// -0.0 is keyed as +0.0, as fim_set_stimuli takes it, so that a vertex given
+// both gets the same seed on both paths.
 __device__ __forceinline__ unsigned long long time_key(double t)
 {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(t);
+  unsigned long long b = (unsigned long long)__double_as_longlong(t);
+  if ((b << 1) == 0ull) b = 0ull;
   return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
 }
 __device__ __forceinline__ double key_time(unsigned long long k)

@@ -111,7 +111,8 @@ int fim_set_conduction_device(fim_solver *s, const double *d_fib, const double *
                               const double *d_ct);
 
 /* Stimuli: n vertices with their start times (the reference seeds every
- * stimulus at time 0, update_events_gpu, cuda_fim.cu:632-683). */
+ * stimulus at time 0, update_events_gpu, cuda_fim.cu:632-683).  A vertex
+ * given several times starts at the earliest; -0.0 counts as +0.0. */
 int fim_set_stimuli(fim_solver *s, int64_t n, const int64_t *vertices, const double *t0);
 
 /* Runs the solve on `stream` (a cudaStream_t, NULL = the solver's working
@@ -158,7 +159,8 @@ int fim_get_stats(const fim_solver *s, fim_stats *out);
  * vertices and 131072 vertex copies (one per submesh holding a vertex),
  * 8192 stimulus entries, 32768 stimulus vertex copies; larger inputs are
  * rejected with FIM_ERR_INVALID_ARGUMENT.  The solver's own buffers, stats
- * and last results are not touched.
+ * and last results are not touched.  A warm start set by fim_set_warm_start
+ * applies here as in fim_solve (it is the caller's own device array).
  *
  * The first call on a device resolves the array's address (and loads its
  * code there); make it before any stream capture.  The array is shared by

@@ -6,7 +6,8 @@
   sources where they lie, plus ref_shim.cpp.  Built only when the reference
   tree is present (it is not shipped with this repository).
 
-Usage: ``python oracle/build.py [--ref-root DIR]``.
+Usage: ``python oracle/build.py [--ref-root DIR]`` (default: $FIM_REFERENCE_ROOT,
+else ``../reference`` beside the repository).
 """
 import argparse
 import os
@@ -14,8 +15,19 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-DEFAULT_REF = "/root/reference"
 CUDA_INC = "/usr/local/cuda/include"
+
+
+def reference_root():
+    """Checkout of the reference: $FIM_REFERENCE_ROOT, else a ``reference``
+    directory beside this repository."""
+    env = os.environ.get("FIM_REFERENCE_ROOT")
+    if env:
+        return env
+    return os.path.normpath(os.path.join(HERE, "..", "..", "reference"))
+
+
+DEFAULT_REF = reference_root()
 
 
 def build_oracle(verbose=False):

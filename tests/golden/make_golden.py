@@ -1,7 +1,7 @@
 """Generates the golden fixtures of tests/golden from the reference itself.
 
-Run in a checkout where the reference tree is present (default
-/root/reference) after ``python oracle/build.py`` has compiled the
+Run in a checkout where the reference tree is present ($FIM_REFERENCE_ROOT,
+else ``../reference`` beside the repository) after ``python oracle/build.py`` has compiled the
 reference's own host code into oracle/_ref/libfimref.so:
 
     python tests/golden/make_golden.py [--ref-root DIR]
@@ -51,7 +51,7 @@ def read_point_data(path, n):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref-root", default="/root/reference")
+    ap.add_argument("--ref-root", default=obuild.reference_root())
     a = ap.parse_args()
     obuild.build_ref(a.ref_root)
     R = O.ref_lib()

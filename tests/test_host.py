@@ -8,6 +8,7 @@ import numpy as np
 import pytest
 
 from conftest import GOLDEN, ROOT
+from oracle.build import reference_root
 
 
 @pytest.fixture(scope="module")
@@ -46,7 +47,7 @@ def test_vtk_reader_roundtrip(F, tmp_path):
 
 
 def test_vtk_reader_matches_reference_on_source_mesh(F):
-    path = "/root/reference/data/ut_mesh/ut_mesh.vtk"
+    path = os.path.join(reference_root(), "data", "ut_mesh", "ut_mesh.vtk")
     if not os.path.exists(path):
         pytest.skip("reference data not present")
     ut = np.load(os.path.join(GOLDEN, "ut_mesh.npz"))
@@ -118,7 +119,8 @@ def test_plan_loader(F, tmp_path):
 
 
 def test_plan_loader_matches_reference(F):
-    cfg, plan = "/root/reference/data/default.cfg", "/root/reference/data/ut_mesh/ut_mesh.plan.json"
+    ref = reference_root()
+    cfg, plan = os.path.join(ref, "data", "default.cfg"), os.path.join(ref, "data", "ut_mesh", "ut_mesh.plan.json")
     if not os.path.exists(plan):
         pytest.skip("reference data not present")
     ut = np.load(os.path.join(GOLDEN, "ut_mesh.npz"))

@@ -72,6 +72,33 @@ def test_noalloc_slab_two_calls(F, torch_cuda):
         _same(s.times(with_state=False), own_b)
 
 
+def test_noalloc_warm_start_and_signed_zero(F, torch_cuda):
+    """A warm start set on the solver applies to both paths alike, and a
+    vertex given both -0.0 and +0.0 is seeded the same way on both."""
+    import fim_mesh
+    torch = torch_cuda
+    c = fim_mesh.slab_case(cells=(30, 12, 5), size=(6.0, 2.4, 1.0), seed=9)
+    v = np.concatenate([c["seed_v"], c["seed_v"][:1], c["seed_v"][:1]]).astype(np.int64)
+    t = np.concatenate([c["seed_t"], [0.0], [-0.0]])
+    t[0] = -0.0
+    with F.Solver() as s:
+        s.set_mesh(c["xyz"], c["tets"])
+        s.set_conduction(c["fib"], c["cf"], c["ct"])
+        cold = _existing(s, torch, v, t)
+        _same(_noalloc(s, torch, v, t), cold)
+        reached = cold < 1e300
+        start = torch.tensor(np.where(reached, np.maximum(cold * 1.05, 0.0), np.finfo(np.float64).max),
+                             dtype=torch.float64, device="cuda")
+        torch.cuda.synchronize()
+        s.set_warm_start(start.data_ptr())
+        warm_a = _existing(s, torch, v, t)
+        got_a = _noalloc(s, torch, v, t)
+        got_b = _noalloc(s, torch, v, t)
+        s.set_warm_start(None)
+        _same(got_a, warm_a)
+        _same(got_b, warm_a)
+
+
 def test_noalloc_submeshes_two_calls(F, torch_cuda):
     """The reference's unit mesh: 4 submeshes, 3 windows of 150000 us with the
     APD reset; the golden stimuli, then a single-vertex stimulus."""
