@@ -16,6 +16,11 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
+# FIM_BUILD_DIR + FIM_BUILD_DEFINES build a variant elsewhere (e.g.
+# FIM_BUILD_DEFINES=FIM_PROBE for per-phase timing of the solve kernel)
+if os.environ.get("FIM_BUILD_DIR"):
+    OUT = os.environ["FIM_BUILD_DIR"]
+DEFINES = ["-D" + x for x in os.environ.get("FIM_BUILD_DEFINES", "").split(",") if x]
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -43,11 +48,11 @@ def _compile(src, verbose):
     if not _needs(obj, [src] + _headers()):
         return obj
     if src.endswith(".cu"):
-        cmd = [NVCC] + ARCH + ["-O3", "-lineinfo", "-fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
-                               "-c", src, "-o", obj]
-    else:
-        cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-fopenmp", "-Wall", "-I" + os.path.join(CUDA_HOME, "include"),
+        cmd = [NVCC] + ARCH + ["-O3", "-lineinfo", "-fmad=false", "-std=c++17", "-Xcompiler", "-fPIC"] + DEFINES + [
                "-c", src, "-o", obj]
+    else:
+        cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-fopenmp", "-Wall", "-I" + os.path.join(CUDA_HOME, "include")] + \
+              DEFINES + ["-c", src, "-o", obj]
     if verbose:
         print(" ".join(cmd), flush=True)
     subprocess.check_call(cmd)

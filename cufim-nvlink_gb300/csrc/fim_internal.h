@@ -70,14 +70,15 @@ struct FimDev {
   const double *cgeo;         // [nC*kCgeoStride] FP64 e13, e23, e34, e12, e14, e24
   const float *cgf;           // [nC*kCgfStride] float screen record: e13..e24 * 2^-k, k, unused
   float *phi_f;               // float copy (round to nearest) of phi, kept in step with it
+  float *phi2_f;              // float copy of phi2
   const int64_t *nptr;        // [nV+1] vertex neighbourhood (self included)
   const int32_t *nbr;
   // state
   double *phi;                // current times
   double *phi2;               // next times (equal to phi outside the updated lists)
-  uint8_t *st;                // state
+  uint32_t *sw;               // state word: state (low 8 bits) | iteration stamp of "marked" << 8
+  uint8_t *st;                // states as bytes, written at the end of a solve (the result)
   uint8_t *tst;               // reference tmp_state
-  int32_t *flag;              // iteration stamp of "marked"
   int32_t *list[3];           // rotating narrow lists
   int32_t *lfrozen;           // frozen this iteration
   int32_t *lmarked;           // marked this iteration
@@ -88,7 +89,12 @@ struct FimDev {
   int32_t nseed;
   const double *phi_init;     // warm start per vertex (nullptr: cold start)
   FimCtl *ctl;
+  unsigned long long *probe;  // per-block phase times (builds with FIM_PROBE only), else nullptr
 };
+
+// Iteration stamps live in the upper 24 bits of the state word.
+constexpr int64_t kMaxStampIterations = (int64_t(1) << 24) - 1;
+constexpr int kProbeSlots = 16;  // phase-time accumulators per block (FIM_PROBE builds)
 
 struct FimParams {
   double dt;            // window length (inf = endless)
@@ -99,6 +105,7 @@ struct FimParams {
   uint64_t timeout_ns;  // per wait
   int32_t withhold_block;  // test hook: block k-1 skips its first barrier arrival (0 = off)
   int32_t exact_all;       // 1: every local solve in FP64, no interval filter
+  int32_t two_phase;       // 1: two grid-synchronised phases per iteration (endless window only)
 };
 
 // Records the message returned by fim_last_error(NULL) on this thread.
@@ -146,8 +153,9 @@ constexpr int64_t kStaticMaxSeedEntries = 32768;   // stimulus entries expanded 
 // Pointers into the fixed scratch of one device.
 struct NoallocScratch {
   double *phi, *phi2;
-  int32_t *flag, *list[3], *lfrozen, *lmarked;
-  float *phi_f;
+  uint32_t *sw;
+  int32_t *list[3], *lfrozen, *lmarked;
+  float *phi_f, *phi2_f;
   uint8_t *st, *tst, *dec, *st_out;
   unsigned long long *key;   // per mesh vertex: earliest stimulus time (order-preserving key)
   int64_t *raw_v;            // stimuli as given

@@ -20,7 +20,8 @@
 //    (cuda_fim.cu:1790-1845), then FIM iterations with the phases of
 //    compute_step (cuda_fim.cu:1992-2334) as global Jacobi steps over
 //    compacted lists (narrow list, vertices frozen this iteration,
-//    neighbours to re-solve), separated by a bounded grid barrier.
+//    neighbours to re-solve), separated by a bounded grid barrier: four
+//    phases per iteration with windows, two with one endless window.
 #include "fim_internal.h"
 #include "fim_filter.cuh"
 
@@ -438,6 +439,33 @@ __device__ bool grid_sync(FimCtl *ctl, uint32_t nblocks, uint64_t timeout_ns, in
 // ---------------------------------------------------------------------------
 // persistent solve
 
+// Phase-time instrumentation (builds with -DFIM_PROBE only): thread 0 of
+// every block adds the time since its previous mark to accumulator k of its
+// block; the marks sit right after block barriers.
+#ifdef FIM_PROBE
+__device__ __forceinline__ void probe_mark(const FimDev &d, int k)
+{
+  __shared__ unsigned long long s_probe_t;
+  if (threadIdx.x == 0) {
+    const unsigned long long t = global_timer();
+    if (k >= 0) d.probe[blockIdx.x * kProbeSlots + k] += t - s_probe_t;
+    s_probe_t = t;
+  }
+}
+__device__ __forceinline__ void probe_count(const FimDev &d, int k)
+{
+  if (threadIdx.x == 0) d.probe[blockIdx.x * kProbeSlots + k] += 1;
+}
+#define PROBE(k) probe_mark(d, (k))
+#define PROBE_COUNT(k) probe_count(d, (k))
+#else
+#define PROBE(k) ((void)0)
+#define PROBE_COUNT(k) ((void)0)
+#endif
+// accumulators
+enum : int { kPrSetup = 0, kPrA, kPrB, kPrS, kPrD, kPrE, kPrMark, kPrBarrier, kPrLight, kPrBatches,
+             kPrPhases };
+
 // Order-preserving map of doubles to unsigned integers, so that the minimum
 // of a vertex's candidates can be formed with integer atomicMin.
 __device__ __forceinline__ unsigned long long dkey(double x)
@@ -469,6 +497,17 @@ constexpr int kQcap = 768;          // exact solves queued per kind and batch (m
 constexpr int kDagWarps = 10;
 constexpr int kDagGroups = kDagWarps * 32 / kDagLanes;
 
+// Update phases.  With windows (finite dt) an iteration runs the reference's
+// four steps as four grid-synchronised phases: kNarrow4 (update the narrow
+// list), the apply + neighbour marking, kMarked4 (re-solve the marked
+// neighbours), the apply + next list.  With one endless window no vertex
+// can leave the narrow list for "next" inside the window, so an iteration
+// needs only two: kNarrow2 updates the narrow list and marks the downwind
+// neighbours of the vertices it freezes, kMarked2 re-solves them, applies
+// everything and builds the next list.
+enum : int { kNarrow4 = 0, kMarked4 = 1, kNarrow2 = 2, kMarked2 = 3 };
+__host__ __device__ constexpr bool is_marked_mode(int m) { return m == kMarked4 || m == kMarked2; }
+
 // Order-preserving map of floats to unsigned integers (for atomicMin).
 __device__ __forceinline__ unsigned int fkey(float x)
 {
@@ -478,6 +517,18 @@ __device__ __forceinline__ unsigned int fkey(float x)
 __device__ __forceinline__ float funkey(unsigned int k)
 {
   return __uint_as_float((k >> 31) ? (k & 0x7fffffffu) : ~k);
+}
+
+// The state word of a vertex copy: state in the low 8 bits, the stamp of the
+// iteration that last marked it for re-solving in the upper 24.
+__device__ __forceinline__ uint32_t sw_state(uint32_t w) { return w & 0xffu; }
+__device__ __forceinline__ uint32_t sw_stamp(uint32_t w) { return w >> 8; }
+__device__ __forceinline__ uint32_t sw_make(uint32_t state, uint32_t stamp) { return state | (stamp << 8); }
+// The state a re-solve phase sees: a vertex marked in this iteration counts
+// as "neig" (cuda_fim.cu:2196-2204), whatever its word still says.
+__device__ __forceinline__ uint32_t sw_seen(uint32_t w, bool marked_mode, uint32_t stamp)
+{
+  return (marked_mode && sw_stamp(w) == stamp) ? (uint32_t)ST_NEIG : sw_state(w);
 }
 
 // Shared memory of one batch of vertex updates.  Phase A loads everything a
@@ -494,6 +545,10 @@ struct BatchSh {
   double old[kSlots];
   unsigned long long res[kSlots];   // dkey of the running minimum (exact values)
   unsigned int bhi[kSlots];         // fkey of a float upper bound of the new time
+  int64_t n0[kSlots];               // kNarrow2: neighbourhood range of each vertex (marking)
+  int32_t ncnt[kSlots];
+  uint8_t tsv[kSlots];              // kMarked2: tmp_state of each vertex
+  int32_t fz[kSlots];               // kNarrow2: slots frozen in this batch
   // per corner of the batch
   union {
     struct {
@@ -513,6 +568,7 @@ struct BatchSh {
   int ntri, ntet, nq[3];
   int next_item;                    // next unclaimed screen item (phase S)
   int nslot;                        // vertices of the current batch
+  int nfz;                          // kNarrow2: frozen slots of the batch
 };
 
 static_assert(sizeof(double) * kDagGroups * kDagSlots <= sizeof(float) * kCornerCap * 6,
@@ -529,8 +585,8 @@ __device__ __forceinline__ int item_slot(uint32_t it) { return (int)(it & 255u);
 __device__ __forceinline__ int item_kind(uint32_t it) { return (int)((it >> 8) & 3u); }
 __device__ __forceinline__ int item_corner(uint32_t it) { return (int)(it >> 10); }
 
-// Appends one item per lane with `need` to a list in shared memory
-// (warp-ballot compaction).  Returns the item's position, or -1.
+// Appends one item per lane with `need` to a list (warp-ballot compaction;
+// every lane of the warp takes part).  Returns the item's position, or -1.
 __device__ __forceinline__ int warp_append(int *counter, bool need, int lane)
 {
   const unsigned mask = __ballot_sync(FULL_MASK, need);
@@ -541,11 +597,12 @@ __device__ __forceinline__ int warp_append(int *counter, bool need, int lane)
   return need ? base + __popc(mask & ((1u << lane) - 1u)) : -1;
 }
 
-// One FP64 local solve of corner c with neighbours nb: kind 0..2 are the
-// triangle solves (1,2), (2,3), (1,3) and kind 3 the tet solve.
-__device__ __forceinline__ double exact_solve(const FimDev &d, int64_t c, int kind, const int32_t *nb)
+// One FP64 local solve of corner c with neighbours nb, on the times ph:
+// kind 0..2 are the triangle solves (1,2), (2,3), (1,3) and kind 3 the tet solve.
+__device__ __forceinline__ double exact_solve(const FimDev &d, const double *ph, int64_t c, int kind,
+                                              const int32_t *nb)
 {
-  const double p1 = __ldcg(d.phi + nb[0]), p2 = __ldcg(d.phi + nb[1]), p3 = __ldcg(d.phi + nb[2]);
+  const double p1 = __ldcg(ph + nb[0]), p2 = __ldcg(ph + nb[1]), p3 = __ldcg(ph + nb[2]);
   const double2 *gp = reinterpret_cast<const double2 *>(d.cgeo + kCgeoStride * c);
   const double2 t0 = __ldg(gp), t1 = __ldg(gp + 1), t2 = __ldg(gp + 2);
   if (kind == 3) return tet_ref(t0.x, t0.y, t1.x, t1.y, t2.x, t2.y, p1, p2, p3);
@@ -563,9 +620,10 @@ __device__ __forceinline__ double exact_solve(const FimDev &d, int64_t c, int ki
 
 // FP64 triangle solve kind 0..2 of corner c (exact_solve without its tet
 // branch, for the warps that run only triangle solves).
-__device__ __forceinline__ double exact_tri(const FimDev &d, int64_t c, int kind, const int32_t *nb)
+__device__ __forceinline__ double exact_tri(const FimDev &d, const double *ph, int64_t c, int kind,
+                                            const int32_t *nb)
 {
-  const double pa = __ldcg(d.phi + (kind == 1 ? nb[1] : nb[0])), pb = __ldcg(d.phi + (kind == 0 ? nb[1] : nb[2]));
+  const double pa = __ldcg(ph + (kind == 1 ? nb[1] : nb[0])), pb = __ldcg(ph + (kind == 0 ? nb[1] : nb[2]));
   const double2 *gp = reinterpret_cast<const double2 *>(d.cgeo + kCgeoStride * c);
   const double2 t0 = __ldg(gp), t1 = __ldg(gp + 1), t2 = __ldg(gp + 2);
   const double e12 = kind == 0 ? t1.y : (kind == 1 ? t0.y : t0.x);
@@ -578,10 +636,10 @@ __device__ __forceinline__ double exact_tri(const FimDev &d, int64_t c, int kind
 // vertex) in a corner record.
 __device__ __forceinline__ int edge_slot(int i) { return i == 0 ? 4 : (i == 1 ? 5 : 2); }
 
-// Edge candidate i (phi of neighbour i + its FP64 edge length) of corner c.
-__device__ __forceinline__ double exact_edge(const FimDev &d, int64_t c, int i, int32_t nbi)
+// Edge candidate i (time of neighbour i + its FP64 edge length) of corner c.
+__device__ __forceinline__ double exact_edge(const FimDev &d, const double *ph, int64_t c, int i, int32_t nbi)
 {
-  return __ldcg(d.phi + nbi) + sqrt(__ldg(d.cgeo + kCgeoStride * c + edge_slot(i)));
+  return __ldcg(ph + nbi) + sqrt(__ldg(d.cgeo + kCgeoStride * c + edge_slot(i)));
 }
 
 // The other three vertices of corner c (from its first-read record, which
@@ -595,27 +653,27 @@ __device__ __forceinline__ void corner_nb(const FimDev &d, int64_t c, int32_t *n
 __device__ __forceinline__ int32_t pick3(const int32_t *nb, int i) { return i == 0 ? nb[0] : (i == 1 ? nb[1] : nb[2]); }
 
 // Evaluates queued item `it` (queue qi) in FP64 and folds it into the minimum.
-__device__ __noinline__ void run_item(const FimDev &d, BatchSh &sh, int qi, uint32_t it)
+__device__ __noinline__ void run_item(const FimDev &d, const double *ph, BatchSh &sh, int qi, uint32_t it)
 {
   const int slot = item_slot(it), kind = item_kind(it), j = item_corner(it);
   const int64_t c = sh.c0[slot] + (j - sh.cp[slot]);
   int32_t nb[3];
   corner_nb(d, c, nb);
-  const double val = qi == 2 ? exact_edge(d, c, kind, pick3(nb, kind)) : exact_solve(d, c, kind, nb);
+  const double val = qi == 2 ? exact_edge(d, ph, c, kind, pick3(nb, kind)) : exact_solve(d, ph, c, kind, nb);
   if (val < FIM_INF) atomicMin(&sh.res[slot], dkey(val));
 }
 
 // Queues an exact solve with lower bound lb (or runs it on the spot when the
 // queue is full).  qi must be the same on every lane of the warp; the item's
 // kind may differ.
-__device__ __forceinline__ void queue_exact(const FimDev &d, BatchSh &sh, bool need, int qi, int kind, int slot, int j,
-                                            float lb, int lane)
+__device__ __forceinline__ void queue_exact(const FimDev &d, const double *ph, BatchSh &sh, bool need, int qi,
+                                            int kind, int slot, int j, float lb, int lane)
 {
   const int pos = warp_append(&sh.nq[qi], need, lane);
   if (pos < 0) return;
   const uint32_t it = make_item(slot, kind, j);
   if (pos < kQcap) { sh.q[qi][pos] = it; sh.qlb[qi][pos] = lb; }
-  else run_item(d, sh, qi, it);
+  else run_item(d, ph, sh, qi, it);
 }
 
 // FP32 screen record of batch corner j: e13, e23, e34, e12, e14, e24 times
@@ -655,19 +713,20 @@ __device__ __forceinline__ CandBound tet_screen_sm(const FimDev &d, const BatchS
 
 // A triangle pair that finds the screen list full: screened (and solved)
 // on the spot; out of line, since it is rare and large.
-__device__ __noinline__ void tri_list_full(const FimDev &d, BatchSh &sh, int j, int k, int slot, float bhi,
-                                           bool exact_all)
+__device__ __noinline__ void tri_list_full(const FimDev &d, const double *ph, BatchSh &sh, int j, int k, int slot,
+                                           float bhi, bool exact_all)
 {
   CandBound cb;
   if (exact_all) { cb.some = CAND_SOME; cb.lb = NAN; cb.ub = INFINITY; }
   else cb = tri_screen_sm(d, sh, j, k);
-  if (cb.some && !(cb.lb > bhi)) run_item(d, sh, 1, make_item(slot, k, j));
+  if (cb.some && !(cb.lb > bhi)) run_item(d, ph, sh, 1, make_item(slot, k, j));
 }
 
 // The corners of a batch beyond kCornerCap (only a batch of one vertex, in
 // slot 0, has them): every solve of them in FP64, the reference's validity
 // on the FP64 times.  Returns the corners with a valid neighbour.
-__device__ __noinline__ int64_t excess_corners(const FimDev &d, BatchSh &sh, int kept, int total, double lower)
+__device__ __noinline__ int64_t excess_corners(const FimDev &d, const double *ph, BatchSh &sh, int kept, int total,
+                                               double lower, bool marked_mode, uint32_t stamp)
 {
   int64_t n_valid = 0;
   for (int j = kept + (int)threadIdx.x; j < total; j += kThreads) {
@@ -677,8 +736,8 @@ __device__ __noinline__ int64_t excess_corners(const FimDev &d, BatchSh &sh, int
     const int32_t nb[3] = {(int32_t)id.x, (int32_t)id.y, (int32_t)id.z};
     uint32_t m = 0;
     for (int i = 0; i < 3; ++i) {
-      const double p = __ldcg(d.phi + nb[i]);
-      if (__ldcg(d.st + nb[i]) >= ST_NARROW && p > lower) {
+      const double p = __ldcg(ph + nb[i]);
+      if (sw_seen(__ldcg(d.sw + nb[i]), marked_mode, stamp) >= ST_NARROW && p > lower) {
         m |= 1u << i;
         atomicMin(&sh.res[slot], dkey(p + sqrt(__ldg(d.cgeo + kCgeoStride * c + edge_slot(i)))));
       }
@@ -687,7 +746,7 @@ __device__ __noinline__ int64_t excess_corners(const FimDev &d, BatchSh &sh, int
     for (int k = 0; k < 4; ++k) {
       const bool use = k == 3 ? m == 7u : (((m >> (k == 1 ? 1 : 0)) & 1u) && ((m >> (k == 0 ? 1 : 2)) & 1u));
       if (!use) continue;
-      const double val = exact_solve(d, c, k, nb);
+      const double val = exact_solve(d, ph, c, k, nb);
       if (val < FIM_INF) atomicMin(&sh.res[slot], dkey(val));
     }
   }
@@ -700,6 +759,22 @@ __device__ __forceinline__ void set_phi(const FimDev &d, int64_t v, double x)
   d.phi[v] = x;
   d.phi_f[v] = (float)x;
 }
+// Writes a time into both time buffers and their float copies.
+__device__ __forceinline__ void set_phi_both(const FimDev &d, int64_t v, double x)
+{
+  const float f = (float)x;
+  d.phi[v] = x; d.phi_f[v] = f;
+  d.phi2[v] = x; d.phi2_f[v] = f;
+}
+
+// Where an update phase appends the vertices of the next narrow list, and
+// the counters of this iteration's lists.
+struct ListOut {
+  int32_t *next;      // next iteration's narrow list
+  int32_t *n_next;    // its length
+  int32_t *n_frozen;  // kNarrow4: vertices frozen now (lfrozen)
+  int32_t *n_marked;  // kNarrow2: neighbours marked now (lmarked)
+};
 
 // One update phase over a vertex list.  Every block takes a contiguous part
 // of the list and processes it in batches of up to kSlots vertices / up to
@@ -721,17 +796,30 @@ __device__ __forceinline__ void set_phi(const FimDev &d, int64_t v, double x)
 //  D -- the queued solves whose lower bound does not exceed the final bhi run
 //       in FP64 (tet prefixes on 8-lane groups and their roots packed from
 //       thread 0; triangles and edges each from a warp boundary);
-//  E -- the reference's per-vertex decision on the exact minimum:
-//   mode 0 -- narrow vertices: window test (next), freeze test
-//             (cuda_fim.cu:2125-2163);
-//   mode 1 -- re-solved neighbours: keep or restore the state
-//             (cuda_fim.cu:2255-2289).
-// The minimum over everything equals the reference's update_per_element
-// minimum over all corners (cuda_fim.h:1362-1411).
-__device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, int32_t n, int mode, double lower,
-                             float lower_lo, float lower_hi, double phi_start, double dt, bool exact_all, int s,
-                             int64_t &n_filtered, int64_t &n_exact)
+//  E -- the reference's per-vertex decision on the exact minimum
+//       (narrow vertices: window test (next), freeze test,
+//       cuda_fim.cu:2125-2163; re-solved neighbours: keep or restore the
+//       state, cuda_fim.cu:2255-2317), per MODE:
+//   kNarrow4 -- new time into phi2, next / frozen-now;
+//   kMarked4 -- new time into phi2, the decided state into dec;
+//   kNarrow2 -- new time into phi2; the vertices frozen now mark their
+//               downwind neighbours (cuda_fim.cu:2172-2205) at once: the
+//               mark is the iteration stamp in the state word, which the
+//               narrow updates running at the same time ignore;
+//   kMarked2 -- new time into both buffers, the state decided and the
+//               vertex appended to the next narrow list.
+// Times are read from phi (narrow modes) or phi2 (kMarked2: the narrow
+// list's new times live there until the phase applies them).  The minimum
+// over everything equals the reference's update_per_element minimum over
+// all corners (cuda_fim.h:1362-1411).
+template <int MODE>
+__device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, int32_t n, double lower,
+                             float lower_lo, float lower_hi, double phi_start, double dt, bool exact_all,
+                             uint32_t stamp, const ListOut &lo_, int64_t &n_filtered, int64_t &n_exact)
 {
+  constexpr bool kMarkedMode = is_marked_mode(MODE);
+  const double *ph = MODE == kMarked2 ? d.phi2 : d.phi;      // times this phase reads
+  const float *phf = MODE == kMarked2 ? d.phi2_f : d.phi_f;
   constexpr int kPer = 3;  // corners per thread and group in phase A
   const int tid = threadIdx.x, lane = tid & 31;
   const int64_t per_block = ((int64_t)n + gridDim.x - 1) / gridDim.x;
@@ -739,21 +827,28 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
   const int64_t lend = min((int64_t)n, lbeg + per_block);
   int64_t pos = lbeg;
   while (pos < lend) {
+    PROBE_COUNT(kPrBatches);
     // batch: the longest run of vertices with <= kCornerCap corners (>= 1 vertex)
     const int cand = (int)min((int64_t)kSlots, lend - pos);
     if (tid < cand) {
       const int32_t v = __ldcg(list + pos + tid);
-      const double old = __ldcg(d.phi + v);
+      const double old = __ldcg(ph + v);
       sh.vtx[tid] = v;
       sh.c0[tid] = d.cptr[v];
       sh.cnt[tid] = (int32_t)(d.cptr[v + 1] - d.cptr[v]);
       sh.old[tid] = old;
       sh.res[tid] = dkey(old);
-      sh.bhi[tid] = fkey(exact_all ? INFINITY : re_hi(re_in(__ldcg(d.phi_f + v))));
+      sh.bhi[tid] = fkey(exact_all ? INFINITY : re_hi(re_in(__ldcg(phf + v))));
+      if (MODE == kNarrow2) {
+        const int64_t a = d.nptr[v];
+        sh.n0[tid] = a;
+        sh.ncnt[tid] = (int32_t)(d.nptr[v + 1] - a);
+      }
+      if (MODE == kMarked2) sh.tsv[tid] = __ldcg(d.tst + v);
     }
     if (tid == 0) {
       sh.cp[0] = 0;
-      sh.ntri = 0; sh.ntet = 0; sh.nq[0] = 0; sh.nq[1] = 0; sh.nq[2] = 0; sh.next_item = 0;
+      sh.ntri = 0; sh.ntet = 0; sh.nq[0] = 0; sh.nq[1] = 0; sh.nq[2] = 0; sh.next_item = 0; sh.nfz = 0;
     }
     __syncthreads();
     if (tid < 32) {
@@ -777,6 +872,7 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
       if (tid == 0) sh.nslot = max(1, fit);
     }
     __syncthreads();
+    PROBE(kPrSetup);
     const int nslot = sh.nslot;
     const int total = sh.cp[nslot];     // may exceed kCornerCap for a single huge vertex
     const int kept = min(total, kCornerCap);
@@ -818,8 +914,8 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
           const int32_t nbs[3] = {(int32_t)h0[r].x, (int32_t)h0[r].y, (int32_t)h0[r].z};
 #pragma unroll
           for (int i = 0; i < 3; ++i) {
-            pf[r][i] = __ldcg(d.phi_f + nbs[i]);
-            stn[r][i] = __ldcg(d.st + nbs[i]);
+            pf[r][i] = __ldcg(phf + nbs[i]);
+            stn[r][i] = (uint8_t)sw_seen(__ldcg(d.sw + nbs[i]), kMarkedMode, stamp);
           }
         }
       }
@@ -850,7 +946,7 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
             else {  // rare: the FP64 time decides
               int32_t nb[3];
               corner_nb(d, sh.c0[slot[r]] + (j - sh.cp[slot[r]]), nb);
-              ok = __ldcg(d.phi + pick3(nb, i)) > lower;
+              ok = __ldcg(ph + pick3(nb, i)) > lower;
             }
           }
           if (ok) {
@@ -866,8 +962,9 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
     }
     // corners beyond kCornerCap (a single vertex with very many corners):
     // every solve of them goes to FP64
-    if (total > kept) n_filtered += excess_corners(d, sh, kept, total, lower);
+    if (total > kept) n_filtered += excess_corners(d, ph, sh, kept, total, lower, kMarkedMode, stamp);
     __syncthreads();
+    PROBE(kPrA);
 
     // B: screen lists
     for (int jb = 0; jb < kept; jb += kThreads) {
@@ -918,7 +1015,7 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
           if (p < kTriCap) {
             sh.tri[p] = (uint32_t)j | ((uint32_t)k << 16);
           } else {  // list full: screen here
-            tri_list_full(d, sh, j, k, slot, bhi, exact_all);
+            tri_list_full(d, ph, sh, j, k, slot, bhi, exact_all);
           }
         }
       }
@@ -929,6 +1026,7 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
       }
     }
     __syncthreads();
+    PROBE(kPrB);
 
     // S: screens over the compacted lists, handed out in chunks to whichever
     // warp is free -- tets first (32 per chunk, one per lane), then triangles
@@ -962,7 +1060,7 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
           for (int i = 0; i < 3; ++i) {
             const float le = in ? re_lo(re_in(sh.pf[j][i]) + re_len(sh.sf[j][i])) : 0.f;
             const bool need = in && ((m >> i) & 1u) && !(le > bhi);
-            queue_exact(d, sh, need, 2, i, slot, j, le, lane);
+            queue_exact(d, ph, sh, need, 2, i, slot, j, le, lane);
           }
           continue;
         }
@@ -982,7 +1080,7 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
             lb = isnan(cb.lb) ? -INFINITY : cb.lb;
             need = cb.some && !(lb > funkey(sh.bhi[slot]));
           }
-          queue_exact(d, sh, need, 0, 3, slot, j, lb, lane);
+          queue_exact(d, ph, sh, need, 0, 3, slot, j, lb, lane);
         } else {
           int jj[2], kk[2], sl[2];
           bool in[2];
@@ -1020,12 +1118,13 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
               lb = isnan(cb[h].lb) ? -INFINITY : cb[h].lb;
               need = cb[h].some && !(lb > funkey(sh.bhi[sl[h]]));
             }
-            queue_exact(d, sh, need, 1, kk[h], sl[h], jj[h], lb, lane);
+            queue_exact(d, ph, sh, need, 1, kk[h], sl[h], jj[h], lb, lane);
           }
         }
       }
     }
     __syncthreads();
+    PROBE(kPrS);
 
     // D: exact solves; tets (a lane group each) from thread 0, triangles and
     // edges each from the next warp boundary
@@ -1057,8 +1156,8 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
               // leaves: e13 e23 e34 e12 e14 e24 p1 p2 (lanes 0..7), p3, 0.5 2.0 1.0 -0.0
               int32_t nb[3];
               corner_nb(d, c, nb);
-              S[gl] = gl < 6 ? __ldg(d.cgeo + kCgeoStride * c + gl) : __ldcg(d.phi + (gl == 6 ? nb[0] : nb[1]));
-              if (gl == 0) S[kDagLeafP1 + 2] = __ldcg(d.phi + nb[2]);
+              S[gl] = gl < 6 ? __ldg(d.cgeo + kCgeoStride * c + gl) : __ldcg(ph + (gl == 6 ? nb[0] : nb[1]));
+              if (gl == 0) S[kDagLeafP1 + 2] = __ldcg(ph + nb[2]);
               else if (gl <= 4) S[kDagLeafConst + gl - 1] = gl == 1 ? 0.5 : (gl == 2 ? 2.0 : (gl == 3 ? 1.0 : -0.0));
             }
           }
@@ -1091,63 +1190,142 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
         const int64_t c = sh.c0[slot] + (jj - sh.cp[slot]);
         int32_t nb[3];
         corner_nb(d, c, nb);
-        const double val = qi == 2 ? exact_edge(d, c, kind, pick3(nb, kind)) : exact_tri(d, c, kind, nb);
+        const double val = qi == 2 ? exact_edge(d, ph, c, kind, pick3(nb, kind)) : exact_tri(d, ph, c, kind, nb);
         if (val < FIM_INF) atomicMin(&sh.res[slot], dkey(val));
         if (qi < 2) ++n_exact;
       }
     }
     __syncthreads();
+    PROBE(kPrD);
 
     // E: decisions
-    if (tid < nslot) {
-      const int slot = tid;
-      const int32_t v = sh.vtx[slot];
-      const double old = sh.old[slot];
-      const double nw = dunkey(sh.res[slot]);
-      d.phi2[v] = nw;
-      if (mode == 0) {
-        d.tst[v] = ST_FAR;
-        if (nw - phi_start > dt) {
-          d.st[v] = ST_NEXT;
-        } else if (fabs(old - nw) < (1e-6 * (1 + (old + nw) * .5))) {
-          d.tst[v] = ST_FROZEN;
-          d.lfrozen[atomicAdd(&d.ctl->n_frozen[s], 1)] = v;
+    if (MODE == kNarrow4 || MODE == kMarked4) {
+      if (tid < nslot) {
+        const int slot = tid;
+        const int32_t v = sh.vtx[slot];
+        const double old = sh.old[slot];
+        const double nw = dunkey(sh.res[slot]);
+        d.phi2[v] = nw;
+        if (MODE == kNarrow4) {
+          d.tst[v] = ST_FAR;
+          if (nw - phi_start > dt) {
+            d.sw[v] = ST_NEXT;
+          } else if (fabs(old - nw) < (1e-6 * (1 + (old + nw) * .5))) {
+            d.tst[v] = ST_FROZEN;
+            d.lfrozen[atomicAdd(lo_.n_frozen, 1)] = v;
+          }
+        } else {
+          d.dec[pos + slot] = (nw < old) ? (uint8_t)ST_NARROW : __ldcg(d.tst + v);
         }
-      } else {
-        d.dec[pos + slot] = (nw < old) ? (uint8_t)ST_NARROW : __ldcg(d.tst + v);
+      }
+    } else if (MODE == kNarrow2) {
+      // the window test never fires (endless window)
+      if (tid < nslot) {
+        const int slot = tid;
+        const int32_t v = sh.vtx[slot];
+        const double old = sh.old[slot];
+        const double nw = dunkey(sh.res[slot]);
+        d.phi2[v] = nw;
+        d.phi2_f[v] = (float)nw;
+        uint8_t t = ST_FAR;
+        if (fabs(old - nw) < (1e-6 * (1 + (old + nw) * .5))) {
+          t = ST_FROZEN;
+          sh.fz[atomicAdd(&sh.nfz, 1)] = slot;
+        }
+        d.tst[v] = t;
+      }
+      __syncthreads();
+      PROBE(kPrE);
+      // the downwind neighbours of the vertices frozen now (not narrow, later
+      // time): stamped in their state word, first stamp wins; a group of
+      // kMarkLanes threads per frozen vertex
+      const int nfz = sh.nfz;
+      for (int g = tid / kMarkLanes; g < nfz; g += kThreads / kMarkLanes) {
+        const int slot = sh.fz[g];
+        const double pn = dunkey(sh.res[slot]);
+        const int64_t k0 = sh.n0[slot], k1 = k0 + sh.ncnt[slot];
+        for (int64_t k = k0 + tid % kMarkLanes; k < k1; k += kMarkLanes) {
+          const int32_t v = __ldg(d.nbr + k);
+          const uint32_t w = __ldcg(d.sw + v);
+          const double pv = __ldcg(d.phi2 + v);
+          if (sw_state(w) != ST_NARROW && sw_stamp(w) != stamp && pn < pv) {
+            if (atomicCAS(d.sw + v, w, sw_make(sw_state(w), stamp)) == w) {
+              d.tst[v] = (uint8_t)sw_state(w);
+              d.lmarked[atomicAdd(lo_.n_marked, 1)] = v;
+            }
+          }
+        }
+      }
+    } else {  // kMarked2
+      if (tid < kSlots) {  // whole warps: the next-list appends are warp-aggregated
+        const int slot = tid;
+        const bool in = slot < nslot;
+        bool push = false;
+        if (in) {
+          const int32_t v = sh.vtx[slot];
+          const double old = sh.old[slot];
+          const double nw = dunkey(sh.res[slot]);
+          const uint8_t tv = sh.tsv[slot];
+          uint8_t sv = (nw < old) ? (uint8_t)ST_NARROW : tv;
+          if (sv == ST_NARROW) {
+            if (tv == ST_FROZEN) sv = ST_FROZEN;
+            else push = true;
+          }
+          d.sw[v] = sw_make(sv, stamp);  // still marked for the re-solves running now
+          set_phi_both(d, v, nw);
+        }
+        const int p = warp_append(lo_.n_next, push, lane);
+        if (p >= 0) lo_.next[p] = sh.vtx[slot];
       }
     }
     __syncthreads();
+    PROBE(MODE == kNarrow2 ? kPrMark : kPrE);
     pos += nslot;
   }
 }
 
+// Grid barrier with its wait accounted in the phase probe.
+__device__ __forceinline__ bool grid_sync_probed(const FimDev &d, uint32_t nblocks, uint64_t timeout_ns, int where)
+{
+  PROBE(kPrLight);  // whatever ran since the last mark
+  const bool ok = grid_sync(d.ctl, nblocks, timeout_ns, where);
+  PROBE(kPrBarrier);
+  (void)d;
+  return ok;
+}
+
+// TWO: two grid-synchronised phases per iteration (one endless window),
+// else four (windows); one instantiation each, so that each holds only the
+// update phases it runs.
+template <bool TWO>
 __global__ void __launch_bounds__(kThreads, 1) fim_solve_kernel(FimDev d, FimParams p)
 {
   FimCtl *ctl = d.ctl;
   const uint32_t nblocks = gridDim.x;
   const int64_t gtid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
+  const int lane = threadIdx.x & 31;
   int64_t my_evals = 0, my_updates = 0, my_exact = 0;
   int where = 0;
   extern __shared__ __align__(16) unsigned char fim_smem[];
   BatchSh &sh = *reinterpret_cast<BatchSh *>(fim_smem);
+  PROBE(-1);
 
   // reset_states_gpu + update_events_gpu: phi = INF, far; seeds narrow.
   // (warm start: every vertex narrow at its given time instead)
   for (int64_t v = gtid; v < d.nV; v += nthreads) {
     const double x = d.phi_init ? d.phi_init[v] : FIM_INF;
-    set_phi(d, v, x); d.phi2[v] = x; d.st[v] = x < FIM_INF ? ST_NARROW : ST_FAR; d.tst[v] = ST_FAR; d.flag[v] = 0;
+    set_phi_both(d, v, x); d.sw[v] = x < FIM_INF ? ST_NARROW : ST_FAR; d.tst[v] = ST_FAR;
   }
   // failure-detection test hook: this block never arrives at the barrier (a
   // flag that nothing sets), so the others' bounded waits must expire
   if (p.withhold_block > 0 && (int64_t)blockIdx.x == (int64_t)p.withhold_block - 1) return;
-  if (!grid_sync(ctl, nblocks, p.timeout_ns, ++where)) return;
+  if (!grid_sync_probed(d, nblocks, p.timeout_ns, ++where)) return;
   for (int64_t i = gtid; i < d.nseed; i += nthreads) {
     const int32_t v = d.seed_v[i];
-    set_phi(d, v, d.seed_t[i]); d.phi2[v] = d.seed_t[i]; d.st[v] = ST_NARROW;
+    set_phi_both(d, v, d.seed_t[i]); d.sw[v] = ST_NARROW;
   }
-  if (!grid_sync(ctl, nblocks, p.timeout_ns, ++where)) return;
+  if (!grid_sync_probed(d, nblocks, p.timeout_ns, ++where)) return;
 
   int64_t it = 0;  // global iteration counter (identical in every block)
   double cur_time = 0.0, phi_start = 0.0;
@@ -1175,25 +1353,25 @@ __global__ void __launch_bounds__(kThreads, 1) fim_solve_kernel(FimDev d, FimPar
         }
         for (int64_t k = k0; k < k1; ++k) {
           const int32_t c = d.gcopy[k];
-          if (mn < __ldcg(d.phi + c)) { set_phi(d, c, mn); d.phi2[c] = mn; d.st[c] = ST_NARROW; }
+          if (mn < __ldcg(d.phi + c)) { set_phi_both(d, c, mn); d.sw[c] = ST_NARROW; }
         }
       }
     }
-    if (!grid_sync(ctl, nblocks, p.timeout_ns, ++where)) return;
+    if (!grid_sync_probed(d, nblocks, p.timeout_ns, ++where)) return;
     // update_states (cuda_fim.cu:1790-1845) -> narrow list of this window
     for (int64_t v = gtid; v < d.nV; v += nthreads) {
-      uint8_t stv = d.st[v];
-      if (stv == ST_NEXT) { stv = ST_NARROW; d.st[v] = stv; }
+      uint8_t stv = (uint8_t)sw_state(d.sw[v]);
+      if (stv == ST_NEXT) { stv = ST_NARROW; d.sw[v] = stv; }
       else if (p.apd >= 0.0 && stv == ST_FROZEN) {
-        if (!(d.phi[v] + p.apd > cur_time)) d.st[v] = ST_TAIL;
+        if (!(d.phi[v] + p.apd > cur_time)) d.sw[v] = ST_TAIL;
       } else if (p.apd >= 0.0 && stv == ST_TAIL) {
         if (!(d.phi[v] + p.apd / 0.91 > cur_time)) {
-          set_phi(d, v, FIM_INF); d.phi2[v] = FIM_INF; d.st[v] = ST_FAR;
+          set_phi_both(d, v, FIM_INF); d.sw[v] = ST_FAR;
         }
       }
       if (stv == ST_NARROW) d.list[s][atomicAdd(&ctl->n_narrow[s], 1)] = (int32_t)v;
     }
-    if (!grid_sync(ctl, nblocks, p.timeout_ns, ++where)) return;
+    if (!grid_sync_probed(d, nblocks, p.timeout_ns, ++where)) return;
 
     int64_t it_window = 0;
     for (;;) {
@@ -1201,90 +1379,145 @@ __global__ void __launch_bounds__(kThreads, 1) fim_solve_kernel(FimDev d, FimPar
       const int s1 = (int)((it + 1) % 3), s2 = (int)((it + 2) % 3);
       const int32_t nn = ld_volatile_i32(&ctl->n_narrow[s]);
       if (nn == 0) break;
-      if (p.max_iter > 0 && it_window >= p.max_iter) {
+      if ((p.max_iter > 0 && it_window >= p.max_iter) || it >= kMaxStampIterations) {
         if (gtid == 0 && atomicCAS(&ctl->error, KERR_NONE, KERR_MAX_ITER) == KERR_NONE) ctl->error_where = where;
         return;
       }
-      const int32_t stamp = (int32_t)(it + 1);
+      const uint32_t stamp = (uint32_t)(it + 1);
       const int32_t *lst = d.list[s];
       int32_t *lnext = d.list[s1];
       if (gtid == 0) { ctl->n_narrow[s2] = 0; ctl->n_frozen[s2] = 0; ctl->n_marked[s2] = 0; }
+      ListOut lo;
+      lo.next = lnext; lo.n_next = &ctl->n_narrow[s1]; lo.n_frozen = &ctl->n_frozen[s];
+      lo.n_marked = &ctl->n_marked[s];
+      PROBE_COUNT(kPrPhases);
 
-      // P1 -- solve on elements + reduce per vertex (cuda_fim.cu:2102-2163)
-      update_phase(d, sh, lst, nn, 0, lower, lower_lo, lower_hi, phi_start, p.dt, p.exact_all != 0, s, my_evals, my_exact);
-      my_updates += (gtid == 0) ? nn : 0;
-      if (!grid_sync(ctl, nblocks, p.timeout_ns, ++where)) return;
+      if (TWO) {
+        // X -- update the narrow list, mark the downwind neighbours of the
+        // vertices frozen now (cuda_fim.cu:2102-2205)
+        update_phase<kNarrow2>(d, sh, lst, nn, lower, lower_lo, lower_hi, phi_start, p.dt, p.exact_all != 0, stamp,
+                               lo, my_evals, my_exact);
+        my_updates += (gtid == 0) ? nn : 0;
+        if (!grid_sync_probed(d, nblocks, p.timeout_ns, ++where)) return;
 
-      // P2 -- apply the narrow times; mark downwind neighbours of the
-      // vertices frozen now (cuda_fim.cu:2172-2205).  The two are
-      // independent: the marking runs on groups of kMarkLanes threads from
-      // the bottom of the grid, the apply on threads from the top, so that
-      // their dependent load chains overlap.
-      for (int64_t i = nthreads - 1 - gtid; i < nn; i += nthreads) {
-        const int32_t v = lst[i];
-        set_phi(d, v, __ldcg(d.phi2 + v));
-      }
-      const int32_t nf = ld_volatile_i32(&ctl->n_frozen[s]);
-      for (int64_t i = gtid / kMarkLanes; i < nf; i += nthreads / kMarkLanes) {
-        const int32_t n = d.lfrozen[i];
-        const double pn = __ldcg(d.phi2 + n);
-        for (int64_t k = d.nptr[n] + gtid % kMarkLanes; k < d.nptr[n + 1]; k += kMarkLanes) {
-          // both loads at once; st[v] changes only after the exchange below,
-          // by its winner, so sv is still v's state there
-          const int32_t v = __ldg(d.nbr + k);
-          const uint8_t sv = __ldcg(d.st + v);
-          const double pv = __ldcg(d.phi2 + v);
-          if (sv != ST_NARROW && pn < pv) {
-            if (atomicExch(d.flag + v, stamp) != stamp) {
-              d.tst[v] = sv;
-              d.st[v] = ST_NEIG;
-              d.lmarked[atomicAdd(&ctl->n_marked[s], 1)] = v;
+        // Y -- apply the narrow list's times and states (the block's share
+        // of the list, cuda_fim.cu:2291-2317), then re-solve the marked
+        // neighbours (cuda_fim.cu:2215-2289), which read the new times from
+        // phi2 and see every marked vertex as "neig"
+        {
+          const int64_t per_block = ((int64_t)nn + gridDim.x - 1) / gridDim.x;
+          const int64_t lbeg = min((int64_t)nn, (int64_t)blockIdx.x * per_block);
+          const int64_t lend = min((int64_t)nn, lbeg + per_block);
+          for (int64_t i0 = lbeg; i0 < lend; i0 += kThreads) {
+            const int64_t i = i0 + threadIdx.x;
+            bool push = false;
+            int32_t v = 0;
+            if (i < lend) {
+              v = lst[i];
+              const uint32_t w = __ldcg(d.sw + v);
+              const uint8_t tv = __ldcg(d.tst + v);
+              const double x = __ldcg(d.phi2 + v);
+              const float xf = __ldcg(d.phi2_f + v);
+              if (sw_stamp(w) != stamp) {  // (a narrow vertex is never marked here)
+                d.phi[v] = x;
+                d.phi_f[v] = xf;
+                if (sw_state(w) == ST_NARROW) {
+                  if (tv == ST_FROZEN) d.sw[v] = ST_FROZEN;
+                  else push = true;
+                }
+              }
+            }
+            const int pp = warp_append(lo.n_next, push, lane);
+            if (pp >= 0) lnext[pp] = v;
+          }
+        }
+        PROBE(kPrLight);
+        const int32_t nm = ld_volatile_i32(&ctl->n_marked[s]);
+        update_phase<kMarked2>(d, sh, d.lmarked, nm, lower, lower_lo, lower_hi, phi_start, p.dt, p.exact_all != 0,
+                               stamp, lo, my_evals, my_exact);
+        my_updates += (gtid == 0) ? nm : 0;
+        ++it;
+        ++it_window;
+        if (!grid_sync_probed(d, nblocks, p.timeout_ns, ++where)) return;
+      } else {
+        // P1 -- solve on elements + reduce per vertex (cuda_fim.cu:2102-2163)
+        update_phase<kNarrow4>(d, sh, lst, nn, lower, lower_lo, lower_hi, phi_start, p.dt, p.exact_all != 0, stamp,
+                               lo, my_evals, my_exact);
+        my_updates += (gtid == 0) ? nn : 0;
+        if (!grid_sync_probed(d, nblocks, p.timeout_ns, ++where)) return;
+
+        // P2 -- apply the narrow times; mark downwind neighbours of the
+        // vertices frozen now (cuda_fim.cu:2172-2205).  The two are
+        // independent: the marking runs on groups of kMarkLanes threads from
+        // the bottom of the grid, the apply on threads from the top, so that
+        // their dependent load chains overlap.
+        for (int64_t i = nthreads - 1 - gtid; i < nn; i += nthreads) {
+          const int32_t v = lst[i];
+          set_phi(d, v, __ldcg(d.phi2 + v));
+        }
+        const int32_t nf = ld_volatile_i32(&ctl->n_frozen[s]);
+        for (int64_t i = gtid / kMarkLanes; i < nf; i += nthreads / kMarkLanes) {
+          const int32_t n = d.lfrozen[i];
+          const double pn = __ldcg(d.phi2 + n);
+          for (int64_t k = d.nptr[n] + gtid % kMarkLanes; k < d.nptr[n + 1]; k += kMarkLanes) {
+            // both loads at once; the word changes only by the exchange below,
+            // so w is still v's word there unless another frozen vertex won
+            const int32_t v = __ldg(d.nbr + k);
+            const uint32_t w = __ldcg(d.sw + v);
+            const double pv = __ldcg(d.phi2 + v);
+            if (sw_state(w) != ST_NARROW && sw_stamp(w) != stamp && pn < pv) {
+              if (atomicCAS(d.sw + v, w, sw_make(ST_NEIG, stamp)) == w) {
+                d.tst[v] = (uint8_t)sw_state(w);
+                d.lmarked[atomicAdd(&ctl->n_marked[s], 1)] = v;
+              }
             }
           }
         }
-      }
-      if (!grid_sync(ctl, nblocks, p.timeout_ns, ++where)) return;
+        if (!grid_sync_probed(d, nblocks, p.timeout_ns, ++where)) return;
 
-      // P3 -- solve elements for neighbours + reduce (cuda_fim.cu:2215-2289)
-      const int32_t nm = ld_volatile_i32(&ctl->n_marked[s]);
-      update_phase(d, sh, d.lmarked, nm, 1, lower, lower_lo, lower_hi, phi_start, p.dt, p.exact_all != 0, s, my_evals, my_exact);
-      my_updates += (gtid == 0) ? nm : 0;
-      if (!grid_sync(ctl, nblocks, p.timeout_ns, ++where)) return;
+        // P3 -- solve elements for neighbours + reduce (cuda_fim.cu:2215-2289)
+        const int32_t nm = ld_volatile_i32(&ctl->n_marked[s]);
+        update_phase<kMarked4>(d, sh, d.lmarked, nm, lower, lower_lo, lower_hi, phi_start, p.dt, p.exact_all != 0,
+                               stamp, lo, my_evals, my_exact);
+        my_updates += (gtid == 0) ? nm : 0;
+        if (!grid_sync_probed(d, nblocks, p.timeout_ns, ++where)) return;
 
-      // P4 -- apply, update neighbour states, next narrow list (cuda_fim.cu:2291-2317):
-      // the re-solved neighbours, then (one index space, so that both run
-      // at once: they touch disjoint vertices) the narrow vertices that
-      // were not re-solved
-      for (int64_t i = gtid; i < (int64_t)nm + nn; i += nthreads) {
-        if (i < nm) {
-          const int32_t v = d.lmarked[i];
-          uint8_t sv = __ldcg(d.dec + i);
-          const uint8_t tv = __ldcg(d.tst + v);
-          set_phi(d, v, __ldcg(d.phi2 + v));
-          if (sv == ST_NARROW) {
-            if (tv == ST_FROZEN) sv = ST_FROZEN;
-            else lnext[atomicAdd(&ctl->n_narrow[s1], 1)] = v;
-          }
-          d.st[v] = sv;
-        } else {
-          // the three loads at once (a re-solved vertex's are not used)
-          const int32_t v = lst[i - nm];
-          const int32_t fv = __ldcg(d.flag + v);
-          const uint8_t sv = __ldcg(d.st + v), tv = __ldcg(d.tst + v);
-          if (fv == stamp) continue;  // re-solved above
-          if (sv == ST_NARROW) {
-            if (tv == ST_FROZEN) d.st[v] = ST_FROZEN;
-            else lnext[atomicAdd(&ctl->n_narrow[s1], 1)] = v;
+        // P4 -- apply, update neighbour states, next narrow list (cuda_fim.cu:2291-2317):
+        // the re-solved neighbours, then (one index space, so that both run
+        // at once: they touch disjoint vertices) the narrow vertices that
+        // were not re-solved
+        for (int64_t i = gtid; i < (int64_t)nm + nn; i += nthreads) {
+          if (i < nm) {
+            const int32_t v = d.lmarked[i];
+            uint8_t sv = __ldcg(d.dec + i);
+            const uint8_t tv = __ldcg(d.tst + v);
+            set_phi(d, v, __ldcg(d.phi2 + v));
+            if (sv == ST_NARROW) {
+              if (tv == ST_FROZEN) sv = ST_FROZEN;
+              else lnext[atomicAdd(&ctl->n_narrow[s1], 1)] = v;
+            }
+            d.sw[v] = sw_make(sv, stamp);  // keeps the stamp: the narrow loop below skips it
+          } else {
+            // the three loads at once (a re-solved vertex's are not used)
+            const int32_t v = lst[i - nm];
+            const uint32_t w = __ldcg(d.sw + v);
+            const uint8_t tv = __ldcg(d.tst + v);
+            if (sw_stamp(w) == stamp) continue;  // re-solved above
+            if (sw_state(w) == ST_NARROW) {
+              if (tv == ST_FROZEN) d.sw[v] = ST_FROZEN;
+              else lnext[atomicAdd(&ctl->n_narrow[s1], 1)] = v;
+            }
           }
         }
+        ++it;
+        ++it_window;
+        if (!grid_sync_probed(d, nblocks, p.timeout_ns, ++where)) return;
       }
-      ++it;
-      ++it_window;
-      if (!grid_sync(ctl, nblocks, p.timeout_ns, ++where)) return;
     }
   }
 
-  // local -> global gather (cuda_fim.cu:2466-2485): min time, max state
+  // local -> global gather (cuda_fim.cu:2466-2485): min time, max state;
+  // with one submesh the states as bytes
   if (d.gptr) {
     for (int64_t g = gtid; g < d.nG; g += nthreads) {
       double mn = FIM_INF;
@@ -1292,13 +1525,15 @@ __global__ void __launch_bounds__(kThreads, 1) fim_solve_kernel(FimDev d, FimPar
       for (int64_t k = d.gptr[g]; k < d.gptr[g + 1]; ++k) {
         const int32_t c = d.gcopy[k];
         const double pc = __ldcg(d.phi + c);
-        const uint8_t sc = __ldcg(d.st + c);
+        const uint8_t sc = (uint8_t)sw_state(__ldcg(d.sw + c));
         if (pc < mn) mn = pc;
         if (sc > mx) mx = sc;
       }
       d.phi_out[g] = mn;
       d.st_out[g] = mx;
     }
+  } else {
+    for (int64_t v = gtid; v < d.nV; v += nthreads) d.st[v] = (uint8_t)sw_state(__ldcg(d.sw + v));
   }
 
   // statistics
@@ -1317,7 +1552,6 @@ __global__ void __launch_bounds__(kThreads, 1) fim_solve_kernel(FimDev d, FimPar
     atomicAdd((unsigned long long *)&ctl->vertex_updates, (unsigned long long)my_updates);
   }
 }
-
 // ---------------------------------------------------------------------------
 // launch wrappers
 
@@ -1339,9 +1573,11 @@ cudaError_t solve_grid_size(int device, int block, int *grid)
   int sms = 0, per_sm = 0;
   cudaError_t e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
   if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(fim_solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(BatchSh));
+  e = cudaFuncSetAttribute(fim_solve_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(BatchSh));
   if (e != cudaSuccess) return e;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fim_solve_kernel, block, sizeof(BatchSh));
+  e = cudaFuncSetAttribute(fim_solve_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(BatchSh));
+  if (e != cudaSuccess) return e;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fim_solve_kernel<false>, block, sizeof(BatchSh));
   if (e != cudaSuccess) return e;
   if (per_sm < 1) per_sm = 1;
   *grid = sms * per_sm;
@@ -1353,8 +1589,8 @@ cudaError_t launch_solve(const FimDev &d, const FimParams &p, int grid, int bloc
   FimDev dd = d;
   FimParams pp = p;
   void *args[] = {&dd, &pp};
-  return cudaLaunchCooperativeKernel((const void *)fim_solve_kernel, dim3(grid), dim3(block), args, sizeof(BatchSh),
-                                     stream);
+  const void *fn = p.two_phase ? (const void *)fim_solve_kernel<true> : (const void *)fim_solve_kernel<false>;
+  return cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(block), args, sizeof(BatchSh), stream);
 }
 
 __global__ void fim_copy_kernel(const double *__restrict__ src, double *__restrict__ dst, int64_t n)

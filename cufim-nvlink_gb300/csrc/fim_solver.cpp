@@ -102,14 +102,16 @@ struct fim_solver {
   DevBuf<int64_t> cidx, cptr, nptr;
   DevBuf<uint4> crec;
   DevBuf<double> cgeo;
-  DevBuf<float> cgf, phi_f;
+  DevBuf<float> cgf, phi_f, phi2_f;
   DevBuf<int32_t> nbr;
   DevBuf<double> fib, cf, ct;
   DevBuf<unsigned long long> bad;  // first invalid tet of the last conduction upload
   // state
   DevBuf<double> phi, phi2;
   DevBuf<uint8_t> st, tst, dec;
-  DevBuf<int32_t> flag, list0, list1, list2, lfrozen, lmarked;
+  DevBuf<uint32_t> sw;
+  DevBuf<int32_t> list0, list1, list2, lfrozen, lmarked;
+  DevBuf<unsigned long long> probe;  // phase times (FIM_PROBE builds)
   DevBuf<int32_t> seed_v;
   DevBuf<double> seed_t;
   int32_t nseed = 0;
@@ -448,10 +450,11 @@ extern "C" int fim_set_mesh(fim_solver *s, int64_t nV, const double *xyz, int64_
   CUDA_TRY(s, s->phi.alloc(nL));
   CUDA_TRY(s, s->phi_f.alloc(nL));
   CUDA_TRY(s, s->phi2.alloc(nL));
+  CUDA_TRY(s, s->phi2_f.alloc(nL));
   CUDA_TRY(s, s->st.alloc(nL));
   CUDA_TRY(s, s->tst.alloc(nL));
   CUDA_TRY(s, s->dec.alloc(nL));
-  CUDA_TRY(s, s->flag.alloc(nL));
+  CUDA_TRY(s, s->sw.alloc(nL));
   CUDA_TRY(s, s->list0.alloc(nL));
   CUDA_TRY(s, s->list1.alloc(nL));
   CUDA_TRY(s, s->list2.alloc(nL));
@@ -613,6 +616,36 @@ extern "C" int fim_set_stimuli(fim_solver *s, int64_t n, const int64_t *vertices
   return FIM_OK;
 }
 
+// Two grid-synchronised phases per FIM iteration need one endless window:
+// only then can no vertex leave the narrow list for "next" in mid-window,
+// which lets the neighbour marking run inside the narrow update.
+static bool two_phase_ok(const FimParams &p)
+{
+  return std::isinf(p.dt) && p.dt > 0.0;
+}
+
+#ifdef FIM_PROBE
+// Per-phase device time of the last solve, averaged over the blocks
+// (instrumented builds only).
+static void print_probe(fim_solver *s)
+{
+  std::vector<unsigned long long> h((size_t)s->grid * kProbeSlots);
+  if (cudaMemcpy(h.data(), s->probe.p, sizeof(unsigned long long) * h.size(), cudaMemcpyDeviceToHost) != cudaSuccess)
+    return;
+  static const char *names[kProbeSlots] = {"setup", "A", "B", "S", "D", "E", "mark", "barrier", "light", "batches",
+                                           "phases", "", "", "", "", ""};
+  std::fprintf(stderr, "probe (mean per block):");
+  for (int k = 0; k < 11; ++k) {
+    double sum = 0.0;
+    for (int b = 0; b < s->grid; ++b) sum += (double)h[(size_t)b * kProbeSlots + k];
+    sum /= s->grid;
+    if (k < 9) std::fprintf(stderr, " %s %.3f ms", names[k], sum * 1e-6);
+    else std::fprintf(stderr, " %s %.1f", names[k], sum);
+  }
+  std::fprintf(stderr, "\n");
+}
+#endif
+
 extern "C" int fim_solve(fim_solver *s, void *stream)
 {
   if (!s) return set_err(nullptr, FIM_ERR_INVALID_ARGUMENT, "fim_solve: solver is NULL");
@@ -624,8 +657,8 @@ extern "C" int fim_solve(fim_solver *s, void *stream)
   d.nV = (int32_t)s->nL; d.nG = (int32_t)s->nV; d.nT = s->nT; d.nC = s->nC;
   d.gptr = s->gptr.p; d.gcopy = s->gcopy.p; d.phi_out = s->phi_out.p; d.st_out = s->st_out.p;
   d.cptr = s->cptr.p; d.crec = s->crec.p; d.cgeo = s->cgeo.p; d.cgf = s->cgf.p; d.nptr = s->nptr.p; d.nbr = s->nbr.p;
-  d.phi_f = s->phi_f.p;
-  d.phi = s->phi.p; d.phi2 = s->phi2.p; d.st = s->st.p; d.tst = s->tst.p; d.flag = s->flag.p;
+  d.phi_f = s->phi_f.p; d.phi2_f = s->phi2_f.p;
+  d.phi = s->phi.p; d.phi2 = s->phi2.p; d.sw = s->sw.p; d.st = s->st.p; d.tst = s->tst.p;
   d.list[0] = s->list0.p; d.list[1] = s->list1.p; d.list[2] = s->list2.p;
   d.lfrozen = s->lfrozen.p; d.lmarked = s->lmarked.p; d.dec = s->dec.p;
   d.seed_v = s->seed_v.p; d.seed_t = s->seed_t.p; d.nseed = s->nseed;
@@ -641,6 +674,12 @@ extern "C" int fim_solve(fim_solver *s, void *stream)
   p.withhold_block = (s->opts.test_withhold_block > 0 && s->opts.test_withhold_block <= s->grid)
                          ? s->opts.test_withhold_block : 0;
   p.exact_all = s->opts.exact_all ? 1 : 0;
+  p.two_phase = two_phase_ok(p) ? 1 : 0;
+#ifdef FIM_PROBE
+  CUDA_TRY(s, s->probe.reserve((size_t)s->grid * kProbeSlots));
+  CUDA_TRY(s, cudaMemsetAsync(s->probe.p, 0, sizeof(unsigned long long) * s->grid * kProbeSlots, st));
+  d.probe = s->probe.p;
+#endif
   CUDA_TRY(s, cudaMemsetAsync(s->ctl.p, 0, sizeof(FimCtl), st));
   CUDA_TRY(s, cudaEventRecord(s->ev0, st));
   CUDA_TRY(s, launch_solve(d, p, s->grid, s->block, st));
@@ -656,6 +695,9 @@ extern "C" int fim_solve(fim_solver *s, void *stream)
   s->stats.exact_evals = s->last_ctl.exact_evals;
   s->stats.grid_blocks = s->grid;
   s->stats.block_threads = s->block;
+#ifdef FIM_PROBE
+  print_probe(s);
+#endif
   if (s->last_ctl.error == KERR_TIMEOUT)
     return set_err(s, FIM_ERR_TIMEOUT, "fim_solve: a grid barrier wait exceeded %.3f s (phase %d)",
                    s->opts.timeout_s, s->last_ctl.error_where);
@@ -762,8 +804,8 @@ extern "C" int fim_solve_noalloc(fim_solver *s, int64_t n, const int64_t *vertic
   d.gptr = s->gptr.p; d.gcopy = s->gcopy.p;
   d.phi_out = multi ? d_phi : nullptr; d.st_out = multi ? sc.st_out : nullptr;
   d.cptr = s->cptr.p; d.crec = s->crec.p; d.cgeo = s->cgeo.p; d.cgf = s->cgf.p; d.nptr = s->nptr.p; d.nbr = s->nbr.p;
-  d.phi_f = sc.phi_f;
-  d.phi = sc.phi; d.phi2 = sc.phi2; d.st = sc.st; d.tst = sc.tst; d.flag = sc.flag;
+  d.phi_f = sc.phi_f; d.phi2_f = sc.phi2_f;
+  d.phi = sc.phi; d.phi2 = sc.phi2; d.sw = sc.sw; d.st = sc.st; d.tst = sc.tst;
   d.list[0] = sc.list[0]; d.list[1] = sc.list[1]; d.list[2] = sc.list[2];
   d.lfrozen = sc.lfrozen; d.lmarked = sc.lmarked; d.dec = sc.dec;
   d.seed_v = sc.seed_v; d.seed_t = sc.seed_t; d.nseed = (int32_t)entries;
@@ -778,6 +820,7 @@ extern "C" int fim_solve_noalloc(fim_solver *s, int64_t n, const int64_t *vertic
   p.timeout_ns = (uint64_t)(s->opts.timeout_s * 1e9);
   p.withhold_block = 0;
   p.exact_all = s->opts.exact_all ? 1 : 0;
+  p.two_phase = two_phase_ok(p) ? 1 : 0;
   CUDA_TRY(s, cudaMemsetAsync(sc.ctl, 0, sizeof(FimCtl), st));
   CUDA_TRY(s, launch_solve(d, p, s->grid, s->block, st));
   if (!multi) CUDA_TRY(s, launch_copy(sc.phi, d_phi, s->nV, st));

@@ -9,8 +9,8 @@
 // module, so it is only loaded on devices where this path is used.
 //
 // Layout (every part starts on a 256-byte boundary): per vertex copy
-// phi, phi2 (f64), flag, list[3], lfrozen, lmarked (i32), phi_f (f32),
-// st, tst, dec (u8); per mesh vertex the gathered states st_out (u8) and
+// phi, phi2 (f64), sw (u32), list[3], lfrozen, lmarked (i32), phi_f,
+// phi2_f (f32), st, tst, dec (u8); per mesh vertex the gathered states st_out (u8) and
 // the stimulus keys (u64); the raw stimuli as given (i64 vertex, f64
 // time), the stimulus entries expanded to vertex copies (i32, f64); the
 // control block FimCtl.
@@ -18,8 +18,8 @@
 // What must start at zero: only the FimCtl block (barrier counter and
 // generation, list counters, error word).  fim_solve_noalloc clears it with
 // cudaMemsetAsync before every launch.  Everything else is written before it
-// is read within one call: the solve kernel resets phi/phi2/st/tst/flag of
-// every copy, the lists are filled behind their counters, and the stimulus
+// is read within one call: the solve kernel resets phi/phi2/sw/tst of every
+// copy, the lists are filled behind their counters, and the stimulus
 // kernel sets the key of every stimulated vertex before it takes minima.
 #include "fim_internal.h"
 
@@ -35,14 +35,15 @@ constexpr size_t kC = (size_t)kStaticMaxCopies;
 constexpr size_t kG = (size_t)kStaticMaxVertices;
 constexpr size_t kOffPhi = 0;
 constexpr size_t kOffPhi2 = kOffPhi + align256(8 * kC);
-constexpr size_t kOffFlag = kOffPhi2 + align256(8 * kC);
-constexpr size_t kOffList0 = kOffFlag + align256(4 * kC);
+constexpr size_t kOffSw = kOffPhi2 + align256(8 * kC);
+constexpr size_t kOffList0 = kOffSw + align256(4 * kC);
 constexpr size_t kOffList1 = kOffList0 + align256(4 * kC);
 constexpr size_t kOffList2 = kOffList1 + align256(4 * kC);
 constexpr size_t kOffFrozen = kOffList2 + align256(4 * kC);
 constexpr size_t kOffMarked = kOffFrozen + align256(4 * kC);
 constexpr size_t kOffPhiF = kOffMarked + align256(4 * kC);
-constexpr size_t kOffSt = kOffPhiF + align256(4 * kC);
+constexpr size_t kOffPhi2F = kOffPhiF + align256(4 * kC);
+constexpr size_t kOffSt = kOffPhi2F + align256(4 * kC);
 constexpr size_t kOffTst = kOffSt + align256(kC);
 constexpr size_t kOffDec = kOffTst + align256(kC);
 constexpr size_t kOffStOut = kOffDec + align256(kC);
@@ -54,7 +55,7 @@ constexpr size_t kOffSeedT = kOffSeedV + align256(4 * (size_t)kStaticMaxSeedEntr
 constexpr size_t kOffCtl = kOffSeedT + align256(8 * (size_t)kStaticMaxSeedEntries);
 constexpr size_t kScratchBytes = kOffCtl + align256(sizeof(FimCtl));
 
-// The scratch itself: about 8 MB, zero at module load.
+// The scratch itself: about 8.5 MB, zero at module load.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
 constexpr int kMaxDevices = 64;
@@ -146,13 +147,14 @@ cudaError_t noalloc_scratch(int device, NoallocScratch *out)
   }
   out->phi = reinterpret_cast<double *>(base + kOffPhi);
   out->phi2 = reinterpret_cast<double *>(base + kOffPhi2);
-  out->flag = reinterpret_cast<int32_t *>(base + kOffFlag);
+  out->sw = reinterpret_cast<uint32_t *>(base + kOffSw);
   out->list[0] = reinterpret_cast<int32_t *>(base + kOffList0);
   out->list[1] = reinterpret_cast<int32_t *>(base + kOffList1);
   out->list[2] = reinterpret_cast<int32_t *>(base + kOffList2);
   out->lfrozen = reinterpret_cast<int32_t *>(base + kOffFrozen);
   out->lmarked = reinterpret_cast<int32_t *>(base + kOffMarked);
   out->phi_f = reinterpret_cast<float *>(base + kOffPhiF);
+  out->phi2_f = reinterpret_cast<float *>(base + kOffPhi2F);
   out->st = base + kOffSt;
   out->tst = base + kOffTst;
   out->dec = base + kOffDec;

@@ -11,7 +11,9 @@ import os
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "_build", "libfim_gb300.so")
+# FIM_GB300_LIB selects another build of the same library (e.g. one compiled
+# with per-phase timing instrumentation)
+LIB_PATH = os.environ.get("FIM_GB300_LIB") or os.path.join(HERE, "_build", "libfim_gb300.so")
 INF = np.finfo(np.float64).max  # the reference's INF (DBL_MAX) for unreached vertices
 
 FIM_OK = 0

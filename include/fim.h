@@ -150,7 +150,7 @@ int fim_get_stats(const fim_solver *s, fim_stats *out);
  * fim_set_stimuli + fim_solve + fim_get_times_device.
  *
  * It calls no allocator: the solve's working set lives in a fixed device
- * array of the library (about 8 MB per device), for callers that must not
+ * array of the library (about 8.5 MB per device), for callers that must not
  * allocate between solves -- e.g. a loop re-solving one mesh for many
  * stimulus sets while other streams run, where fim_set_stimuli grows its
  * seed buffers whenever a stimulus set is larger than all before it (a
