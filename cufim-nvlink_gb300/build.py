@@ -25,7 +25,8 @@ CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SOURCES = ["fim_kernels.cu", "fim_static.cu", "fim_mlp.cu"]
+CU_SOURCES = ["fim_kernels.cu", "fim_solve_s192.cu", "fim_solve_s160.cu", "fim_solve_s96.cu", "fim_static.cu",
+              "fim_mlp.cu"]
 CPP_SOURCES = ["fim_solver.cpp", "fim_io.cpp", "cuda_solver_fim.cpp"]
 CLI_SOURCES = ["fim_cli.cpp"]
 
@@ -38,7 +39,7 @@ def _needs(out, deps):
 
 
 def _headers():
-    hs = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".h")]
+    hs = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh", ".inc"))]
     hs.append(os.path.join(HERE, "..", "include", "fim.h"))
     return hs
 

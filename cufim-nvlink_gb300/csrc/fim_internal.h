@@ -106,7 +106,12 @@ struct FimParams {
   int32_t withhold_block;  // test hook: block k-1 skips its first barrier arrival (0 = off)
   int32_t exact_all;       // 1: every local solve in FP64, no interval filter
   int32_t two_phase;       // 1: two grid-synchronised phases per iteration (endless window only)
+  int32_t dag_warps;       // warps running the FP64 tet prefix groups of a batch (1..kDagWarpsMax)
 };
+
+// Most warps of a batch that run FP64 tet prefix groups (the scratch is
+// sized for it).
+constexpr int kDagWarpsMax = 12;
 
 // Records the message returned by fim_last_error(NULL) on this thread.
 void set_last_error(const char *msg);
@@ -118,10 +123,20 @@ void set_last_error(const char *msg);
 cudaError_t launch_metric(const int32_t *tslots, const int64_t *cidx, const double *xyz,
                           const double *fib, const double *cf, const double *ct, int64_t e0, int64_t e1,
                           double *cgeo, float *cgf, uint4 *crec, unsigned long long *bad, cudaStream_t stream);
-// Persistent cooperative solve.
-cudaError_t launch_solve(const FimDev &d, const FimParams &p, int grid, int block, cudaStream_t stream);
-// Occupancy-derived grid size for the cooperative launch.
-cudaError_t solve_grid_size(int device, int block, int *grid);
+// The persistent cooperative solve is compiled once per batch shape
+// (fim_solve_s*.cu: vertices x corners a block stages per batch); the
+// autotuner picks the shape, the grid and the tet-prefix warps per problem.
+constexpr int kNumShapes = 3;
+struct ShapeDesc {
+  const char *name;
+  int slots;    // vertices per batch
+  int corners;  // corners per batch
+};
+extern const ShapeDesc kShapes[kNumShapes];
+// Sets the shape's shared-memory size and returns its largest co-resident grid.
+cudaError_t solve_prepare(int shape, int device, int block, int *max_grid);
+// Persistent cooperative solve with batch shape `shape`.
+cudaError_t launch_solve(const FimDev &d, const FimParams &p, int shape, int grid, int block, cudaStream_t stream);
 // Writes phi (any order) into out.
 cudaError_t launch_copy(const double *src, double *dst, int64_t n, cudaStream_t stream);
 

@@ -35,6 +35,8 @@ namespace {
 
 thread_local std::string g_last_error;
 
+constexpr int kDefaultDagWarps = 10;
+
 template <class T>
 struct DevBuf {
   T *p = nullptr;
@@ -83,7 +85,13 @@ struct fim_solver {
   cudaStream_t copy_stream = nullptr;
   cudaEvent_t ev_dep = nullptr, ev_chunk[kCondChunks] = {};
   std::string err;
-  int grid = 0, block = kSolveThreads;
+  int block = kSolveThreads;
+  // launch configuration of the solve kernel: batch shape, grid, tet-prefix
+  // warps (defaults, or the autotuner's choice for the staged problem)
+  int max_grid[kNumShapes] = {};
+  int shape = 0, grid = 0, dag_warps = kDefaultDagWarps;
+  bool tuned = false;
+  fim_tune_info tune{};
 
   // mesh (nL vertex copies: nL == nV with one submesh)
   int64_t nV = 0, nT = 0, nC = 0, nL = 0;
@@ -162,6 +170,20 @@ extern "C" const char *fim_last_error(const fim_solver *s)
   return g_last_error.c_str();
 }
 
+// Loads every batch shape of the solve kernel and records its largest
+// co-resident grid; the default configuration is shape 0 on its full grid.
+static cudaError_t prepare_shapes(fim_solver *s)
+{
+  for (int k = 0; k < kNumShapes; ++k) {
+    const cudaError_t e = solve_prepare(k, s->device, s->block, &s->max_grid[k]);
+    if (e != cudaSuccess) return e;
+  }
+  s->shape = 0;
+  s->grid = s->max_grid[0];
+  s->dag_warps = kDefaultDagWarps;
+  return cudaSuccess;
+}
+
 static cudaError_t create_chunk_events(fim_solver *s)
 {
   for (cudaEvent_t &ev : s->ev_chunk) {
@@ -197,7 +219,7 @@ extern "C" int fim_create(const fim_opts *opts, fim_solver **out)
       (e = cudaStreamCreateWithFlags(&s->copy_stream, cudaStreamDefault)) != cudaSuccess ||
       (e = cudaEventCreateWithFlags(&s->ev_dep, cudaEventDisableTiming)) != cudaSuccess ||
       (e = create_chunk_events(s)) != cudaSuccess || (e = s->bad.alloc(1)) != cudaSuccess ||
-      (e = solve_grid_size(s->device, s->block, &s->grid)) != cudaSuccess || (e = s->ctl.alloc(1)) != cudaSuccess) {
+      (e = prepare_shapes(s)) != cudaSuccess || (e = s->ctl.alloc(1)) != cudaSuccess) {
     int rc = set_err(nullptr, FIM_ERR_CUDA, "fim_create: %s", cudaGetErrorString(e));
     fim_destroy(s);
     return rc;
@@ -428,6 +450,10 @@ extern "C" int fim_set_mesh(fim_solver *s, int64_t nV, const double *xyz, int64_
 
   CUDA_TRY(s, cudaSetDevice(s->device));
   s->warm = nullptr;  // a warm start belongs to the previous mesh
+  if (s->tuned) {      // so does a tuned launch configuration
+    s->tuned = false;
+    s->shape = 0; s->grid = s->max_grid[0]; s->dag_warps = kDefaultDagWarps;
+  }
   s->have_mesh = s->have_cond = s->have_stim = s->solved = false;
   s->nV = nV; s->nT = nT; s->nC = nC; s->nL = nL;
   s->n_submeshes = S.n_submeshes;
@@ -627,9 +653,9 @@ static bool two_phase_ok(const FimParams &p)
 #ifdef FIM_PROBE
 // Per-phase device time of the last solve, averaged over the blocks
 // (instrumented builds only).
-static void print_probe(fim_solver *s)
+static void print_probe(fim_solver *s, int grid)
 {
-  std::vector<unsigned long long> h((size_t)s->grid * kProbeSlots);
+  std::vector<unsigned long long> h((size_t)grid * kProbeSlots);
   if (cudaMemcpy(h.data(), s->probe.p, sizeof(unsigned long long) * h.size(), cudaMemcpyDeviceToHost) != cudaSuccess)
     return;
   static const char *names[kProbeSlots] = {"setup", "A", "B", "S", "D", "E", "mark", "barrier", "light", "batches",
@@ -637,8 +663,8 @@ static void print_probe(fim_solver *s)
   std::fprintf(stderr, "probe (mean per block):");
   for (int k = 0; k < 11; ++k) {
     double sum = 0.0;
-    for (int b = 0; b < s->grid; ++b) sum += (double)h[(size_t)b * kProbeSlots + k];
-    sum /= s->grid;
+    for (int b = 0; b < grid; ++b) sum += (double)h[(size_t)b * kProbeSlots + k];
+    sum /= grid;
     if (k < 9) std::fprintf(stderr, " %s %.3f ms", names[k], sum * 1e-6);
     else std::fprintf(stderr, " %s %.1f", names[k], sum);
   }
@@ -646,13 +672,11 @@ static void print_probe(fim_solver *s)
 }
 #endif
 
-extern "C" int fim_solve(fim_solver *s, void *stream)
+static int tune_solver(fim_solver *s, cudaStream_t st);
+
+// One solve with launch configuration (shape, grid, dag_warps).
+static int run_solve(fim_solver *s, cudaStream_t st, int shape, int grid, int dag_warps)
 {
-  if (!s) return set_err(nullptr, FIM_ERR_INVALID_ARGUMENT, "fim_solve: solver is NULL");
-  if (!s->have_mesh || !s->have_cond || !s->have_stim)
-    return set_err(s, FIM_ERR_NOT_READY, "fim_solve: mesh, conduction and stimuli must be set first");
-  CUDA_TRY(s, cudaSetDevice(s->device));
-  cudaStream_t st = stream ? (cudaStream_t)stream : s->stream;
   FimDev d{};
   d.nV = (int32_t)s->nL; d.nG = (int32_t)s->nV; d.nT = s->nT; d.nC = s->nC;
   d.gptr = s->gptr.p; d.gcopy = s->gcopy.p; d.phi_out = s->phi_out.p; d.st_out = s->st_out.p;
@@ -671,18 +695,19 @@ extern "C" int fim_solve(fim_solver *s, void *stream)
   p.apd = s->opts.apd;
   p.max_iter = s->opts.max_iterations > 0 ? s->opts.max_iterations : 10000000;
   p.timeout_ns = (uint64_t)(s->opts.timeout_s * 1e9);
-  p.withhold_block = (s->opts.test_withhold_block > 0 && s->opts.test_withhold_block <= s->grid)
+  p.withhold_block = (s->opts.test_withhold_block > 0 && s->opts.test_withhold_block <= grid)
                          ? s->opts.test_withhold_block : 0;
   p.exact_all = s->opts.exact_all ? 1 : 0;
   p.two_phase = two_phase_ok(p) ? 1 : 0;
+  p.dag_warps = dag_warps;
 #ifdef FIM_PROBE
-  CUDA_TRY(s, s->probe.reserve((size_t)s->grid * kProbeSlots));
-  CUDA_TRY(s, cudaMemsetAsync(s->probe.p, 0, sizeof(unsigned long long) * s->grid * kProbeSlots, st));
+  CUDA_TRY(s, s->probe.reserve((size_t)grid * kProbeSlots));
+  CUDA_TRY(s, cudaMemsetAsync(s->probe.p, 0, sizeof(unsigned long long) * grid * kProbeSlots, st));
   d.probe = s->probe.p;
 #endif
   CUDA_TRY(s, cudaMemsetAsync(s->ctl.p, 0, sizeof(FimCtl), st));
   CUDA_TRY(s, cudaEventRecord(s->ev0, st));
-  CUDA_TRY(s, launch_solve(d, p, s->grid, s->block, st));
+  CUDA_TRY(s, launch_solve(d, p, shape, grid, s->block, st));
   CUDA_TRY(s, cudaEventRecord(s->ev1, st));
   CUDA_TRY(s, cudaMemcpyAsync(&s->last_ctl, s->ctl.p, sizeof(FimCtl), cudaMemcpyDeviceToHost, st));
   CUDA_TRY(s, cudaStreamSynchronize(st));
@@ -693,10 +718,13 @@ extern "C" int fim_solve(fim_solver *s, void *stream)
   s->stats.vertex_updates = s->last_ctl.vertex_updates;
   s->stats.corner_evals = s->last_ctl.corner_evals;
   s->stats.exact_evals = s->last_ctl.exact_evals;
-  s->stats.grid_blocks = s->grid;
+  s->stats.grid_blocks = grid;
   s->stats.block_threads = s->block;
+  s->stats.batch_slots = kShapes[shape].slots;
+  s->stats.batch_corners = kShapes[shape].corners;
+  s->stats.dag_warps = dag_warps;
 #ifdef FIM_PROBE
-  print_probe(s);
+  print_probe(s, grid);
 #endif
   if (s->last_ctl.error == KERR_TIMEOUT)
     return set_err(s, FIM_ERR_TIMEOUT, "fim_solve: a grid barrier wait exceeded %.3f s (phase %d)",
@@ -705,6 +733,143 @@ extern "C" int fim_solve(fim_solver *s, void *stream)
     return set_err(s, FIM_ERR_MAX_ITERATIONS, "fim_solve: iteration cap %lld reached in a window",
                    (long long)p.max_iter);
   s->solved = true;
+  return FIM_OK;
+}
+
+extern "C" int fim_solve(fim_solver *s, void *stream)
+{
+  if (!s) return set_err(nullptr, FIM_ERR_INVALID_ARGUMENT, "fim_solve: solver is NULL");
+  if (!s->have_mesh || !s->have_cond || !s->have_stim)
+    return set_err(s, FIM_ERR_NOT_READY, "fim_solve: mesh, conduction and stimuli must be set first");
+  CUDA_TRY(s, cudaSetDevice(s->device));
+  cudaStream_t st = stream ? (cudaStream_t)stream : s->stream;
+  if (s->opts.autotune && !s->tuned) {
+    const int rc = tune_solver(s, st);
+    if (rc != FIM_OK) return rc;
+  }
+  return run_solve(s, st, s->shape, s->grid, s->dag_warps);
+}
+
+// ---------------------------------------------------------------------------
+// autotuner (replaces the reference's external partition and its fixed
+// block size, types.cpp:306-570, cuda_fim.cu:2435)
+//
+// The solve's speed depends on the problem: how many vertices a FIM
+// iteration updates (the front), how many corners they have, how many of
+// their local solves survive the FP32 screens.  The tuner times full solves
+// of the staged problem under candidate launch configurations and keeps the
+// fastest: first the batch shape (vertices x corners a block stages at once)
+// on its full grid, then the grid (fewer persistent blocks cost less per
+// grid barrier and give each block more vertices), then the number of warps
+// running the FP64 tet prefixes.  Every configuration computes the same
+// times bit for bit; only the speed differs.
+
+// Device time of one solve under a configuration (the better of two runs
+// for short solves).
+static int time_config(fim_solver *s, cudaStream_t st, int shape, int grid, int dag, double *ms)
+{
+  int rc = run_solve(s, st, shape, grid, dag);
+  if (rc != FIM_OK) return rc;
+  double best = s->stats.solve_ms;
+  if (best < 200.0) {
+    rc = run_solve(s, st, shape, grid, dag);
+    if (rc != FIM_OK) return rc;
+    best = std::min(best, s->stats.solve_ms);
+  }
+  *ms = best;
+  return FIM_OK;
+}
+
+static int tune_solver(fim_solver *s, cudaStream_t st)
+{
+  int n = 0;
+  double def_ms = 0.0;
+  int rc = time_config(s, st, 0, s->max_grid[0], kDefaultDagWarps, &def_ms);
+  if (rc != FIM_OK) return rc;
+  ++n;
+  int b_shape = 0, b_grid = s->max_grid[0], b_dag = kDefaultDagWarps;
+  double b_ms = def_ms;
+  auto consider = [&](int shape, int grid, int dag) -> int {
+    double ms = 0.0;
+    const int r = time_config(s, st, shape, grid, dag, &ms);
+    if (r != FIM_OK) return r;
+    ++n;
+    if (ms < b_ms) { b_ms = ms; b_shape = shape; b_grid = grid; b_dag = dag; }
+    return FIM_OK;
+  };
+  for (int k = 1; k < kNumShapes; ++k)
+    if ((rc = consider(k, s->max_grid[k], kDefaultDagWarps)) != FIM_OK) return rc;
+  const int full = s->max_grid[b_shape];
+  for (int div : {2, 4})
+    if (full / div >= 1 && (rc = consider(b_shape, full / div, kDefaultDagWarps)) != FIM_OK) return rc;
+  const int g = b_grid;
+  for (int dag : {6, 8, 12})
+    if ((rc = consider(b_shape, g, dag)) != FIM_OK) return rc;
+  s->shape = b_shape; s->grid = b_grid; s->dag_warps = b_dag;
+  s->tuned = true;
+  s->tune.batch_slots = kShapes[b_shape].slots;
+  s->tune.batch_corners = kShapes[b_shape].corners;
+  s->tune.grid_blocks = b_grid;
+  s->tune.dag_warps = b_dag;
+  s->tune.default_ms = def_ms;
+  s->tune.tuned_ms = b_ms;
+  s->tune.candidates = n;
+  return FIM_OK;
+}
+
+extern "C" int fim_autotune(fim_solver *s, void *stream, fim_tune_info *info)
+{
+  if (!s) return set_err(nullptr, FIM_ERR_INVALID_ARGUMENT, "fim_autotune: solver is NULL");
+  if (!s->have_mesh || !s->have_cond || !s->have_stim)
+    return set_err(s, FIM_ERR_NOT_READY, "fim_autotune: mesh, conduction and stimuli must be set first");
+  CUDA_TRY(s, cudaSetDevice(s->device));
+  const int rc = tune_solver(s, stream ? (cudaStream_t)stream : s->stream);
+  if (rc != FIM_OK) return rc;
+  if (info) *info = s->tune;
+  return FIM_OK;
+}
+
+extern "C" int fim_set_tune(fim_solver *s, const fim_tune_info *cfg)
+{
+  if (!s) return set_err(nullptr, FIM_ERR_INVALID_ARGUMENT, "fim_set_tune: solver is NULL");
+  if (!cfg) {  // back to the default configuration
+    s->tuned = false;
+    s->shape = 0; s->grid = s->max_grid[0]; s->dag_warps = kDefaultDagWarps;
+    return FIM_OK;
+  }
+  int shape = -1;
+  for (int k = 0; k < kNumShapes; ++k)
+    if (kShapes[k].slots == cfg->batch_slots && kShapes[k].corners == cfg->batch_corners) shape = k;
+  if (shape < 0) {
+    std::string have;
+    for (int k = 0; k < kNumShapes; ++k) have += std::string(k ? ", " : "") + kShapes[k].name;
+    return set_err(s, FIM_ERR_INVALID_ARGUMENT, "fim_set_tune: no batch shape %dx%d (compiled: %s)", cfg->batch_slots,
+                   cfg->batch_corners, have.c_str());
+  }
+  if (cfg->grid_blocks < 1 || cfg->grid_blocks > s->max_grid[shape])
+    return set_err(s, FIM_ERR_INVALID_ARGUMENT, "fim_set_tune: grid %d outside [1,%d]", cfg->grid_blocks,
+                   s->max_grid[shape]);
+  if (cfg->dag_warps < 1 || cfg->dag_warps > kDagWarpsMax)
+    return set_err(s, FIM_ERR_INVALID_ARGUMENT, "fim_set_tune: dag_warps %d outside [1,%d]", cfg->dag_warps,
+                   kDagWarpsMax);
+  s->shape = shape; s->grid = cfg->grid_blocks; s->dag_warps = cfg->dag_warps;
+  s->tuned = true;
+  s->tune = *cfg;
+  return FIM_OK;
+}
+
+extern "C" int fim_get_tune(const fim_solver *s, fim_tune_info *info)
+{
+  if (!s || !info) return set_err(nullptr, FIM_ERR_INVALID_ARGUMENT, "fim_get_tune: NULL argument");
+  if (s->tuned) {
+    *info = s->tune;
+  } else {
+    std::memset(info, 0, sizeof(*info));
+    info->batch_slots = kShapes[s->shape].slots;
+    info->batch_corners = kShapes[s->shape].corners;
+    info->grid_blocks = s->grid;
+    info->dag_warps = s->dag_warps;
+  }
   return FIM_OK;
 }
 
@@ -821,8 +986,9 @@ extern "C" int fim_solve_noalloc(fim_solver *s, int64_t n, const int64_t *vertic
   p.withhold_block = 0;
   p.exact_all = s->opts.exact_all ? 1 : 0;
   p.two_phase = two_phase_ok(p) ? 1 : 0;
+  p.dag_warps = s->dag_warps;
   CUDA_TRY(s, cudaMemsetAsync(sc.ctl, 0, sizeof(FimCtl), st));
-  CUDA_TRY(s, launch_solve(d, p, s->grid, s->block, st));
+  CUDA_TRY(s, launch_solve(d, p, s->shape, s->grid, s->block, st));
   if (!multi) CUDA_TRY(s, launch_copy(sc.phi, d_phi, s->nV, st));
   FimCtl ctl{};
   CUDA_TRY(s, cudaMemcpyAsync(&ctl, sc.ctl, sizeof(FimCtl), cudaMemcpyDeviceToHost, st));
@@ -953,20 +1119,40 @@ extern "C" int fim_batch_add(fim_batch *b, int64_t nV, const double *xyz, int64_
   return FIM_OK;
 }
 
+// Stages every problem of the batch as one disjoint mesh (once after adds).
+static int batch_stage(fim_batch *b, const char *who)
+{
+  if (b->staged) return FIM_OK;
+  fim_solver *s = b->s;
+  int rc;
+  const int64_t nV = (int64_t)b->xyz.size() / 3, nT = (int64_t)b->tets.size() / 4;
+  if ((rc = fim_set_mesh(s, nV, b->xyz.data(), nT, b->tets.data(), nullptr)) != FIM_OK ||
+      (rc = fim_set_conduction(s, b->fib.data(), b->cf.data(), b->ct.data())) != FIM_OK ||
+      (rc = fim_set_stimuli(s, (int64_t)b->stim_v.size(), b->stim_v.data(), b->stim_t.data())) != FIM_OK)
+    return batch_err(b, rc, "%s: %s", who, fim_last_error(s));
+  b->staged = true;
+  return FIM_OK;
+}
+
+extern "C" int fim_batch_autotune(fim_batch *b, void *stream, fim_tune_info *info)
+{
+  if (!b) return batch_err(nullptr, FIM_ERR_INVALID_ARGUMENT, "fim_batch_autotune: batch is NULL");
+  if (b->probs.empty()) return batch_err(b, FIM_ERR_NOT_READY, "fim_batch_autotune: no problems added");
+  int rc = batch_stage(b, "fim_batch_autotune");
+  if (rc != FIM_OK) return rc;
+  if ((rc = fim_autotune(b->s, stream, info)) != FIM_OK)
+    return batch_err(b, rc, "fim_batch_autotune: %s", fim_last_error(b->s));
+  b->solved = false;
+  return FIM_OK;
+}
+
 extern "C" int fim_batch_solve(fim_batch *b, void *stream)
 {
   if (!b) return batch_err(nullptr, FIM_ERR_INVALID_ARGUMENT, "fim_batch_solve: batch is NULL");
   if (b->probs.empty()) return batch_err(b, FIM_ERR_NOT_READY, "fim_batch_solve: no problems added");
   fim_solver *s = b->s;
-  int rc;
-  if (!b->staged) {
-    const int64_t nV = (int64_t)b->xyz.size() / 3, nT = (int64_t)b->tets.size() / 4;
-    if ((rc = fim_set_mesh(s, nV, b->xyz.data(), nT, b->tets.data(), nullptr)) != FIM_OK ||
-        (rc = fim_set_conduction(s, b->fib.data(), b->cf.data(), b->ct.data())) != FIM_OK ||
-        (rc = fim_set_stimuli(s, (int64_t)b->stim_v.size(), b->stim_v.data(), b->stim_t.data())) != FIM_OK)
-      return batch_err(b, rc, "fim_batch_solve: %s", fim_last_error(s));
-    b->staged = true;
-  }
+  int rc = batch_stage(b, "fim_batch_solve");
+  if (rc != FIM_OK) return rc;
   if ((rc = fim_solve(s, stream)) != FIM_OK) return batch_err(b, rc, "fim_batch_solve: %s", fim_last_error(s));
   try {
     b->phi.resize(b->xyz.size() / 3);

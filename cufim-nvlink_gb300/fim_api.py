@@ -29,7 +29,8 @@ EXPORTS = ["fim_default_opts", "fim_create", "fim_destroy", "fim_last_error", "f
            "fim_read_tags", "fim_load_plan", "fim_set_stream", "fim_solve_noalloc", "fim_batch_create",
            "fim_batch_destroy", "fim_batch_last_error", "fim_batch_add", "fim_batch_solve", "fim_batch_get_times",
            "fim_batch_get_stats", "fim_mlp_create", "fim_mlp_destroy", "fim_mlp_set_params", "fim_mlp_get_params",
-           "fim_mlp_gradients", "fim_mlp_train_step", "fim_mlp_predict", "fim_features", "fim_set_warm_start"]
+           "fim_mlp_gradients", "fim_mlp_train_step", "fim_mlp_predict", "fim_features", "fim_set_warm_start",
+           "fim_autotune", "fim_get_tune", "fim_set_tune", "fim_batch_autotune"]
 MLP_INPUTS = 64
 MLP_PARAMS = 41473
 
@@ -37,13 +38,21 @@ MLP_PARAMS = 41473
 class FimOpts(C.Structure):
     _fields_ = [("device", C.c_int), ("dt", C.c_double), ("n_steps", C.c_int), ("front_width", C.c_double),
                 ("apd", C.c_double), ("max_iterations", C.c_int64), ("timeout_s", C.c_double),
-                ("verbose", C.c_int), ("test_withhold_block", C.c_int), ("exact_all", C.c_int)]
+                ("verbose", C.c_int), ("test_withhold_block", C.c_int), ("exact_all", C.c_int),
+                ("autotune", C.c_int)]
 
 
 class FimStats(C.Structure):
     _fields_ = [("iterations", C.c_int64), ("vertex_updates", C.c_int64), ("corner_evals", C.c_int64),
                 ("exact_evals", C.c_int64), ("solve_ms", C.c_double), ("metric_ms", C.c_double), ("n_corners", C.c_int64),
-                ("grid_blocks", C.c_int), ("block_threads", C.c_int)]
+                ("grid_blocks", C.c_int), ("block_threads", C.c_int), ("batch_slots", C.c_int),
+                ("batch_corners", C.c_int), ("dag_warps", C.c_int)]
+
+
+class FimTuneInfo(C.Structure):
+    _fields_ = [("batch_slots", C.c_int), ("batch_corners", C.c_int), ("grid_blocks", C.c_int),
+                ("dag_warps", C.c_int), ("default_ms", C.c_double), ("tuned_ms", C.c_double),
+                ("candidates", C.c_int)]
 
 
 class FimPlanInfo(C.Structure):
@@ -103,6 +112,10 @@ def lib():
         L.fim_mlp_predict.argtypes = [vp, i64, vp, vp]
         L.fim_features.argtypes = [vp, vp, P(f32)]
         L.fim_set_warm_start.argtypes = [vp, vp]
+        L.fim_autotune.argtypes = [vp, vp, P(FimTuneInfo)]
+        L.fim_get_tune.argtypes = [vp, P(FimTuneInfo)]
+        L.fim_set_tune.argtypes = [vp, P(FimTuneInfo)]
+        L.fim_batch_autotune.argtypes = [vp, vp, P(FimTuneInfo)]
         L.fim_vtk_read.argtypes = [C.c_char_p, P(i64), P(i64), P(d), P(i64), P(i32)]
         L.fim_vtk_write.argtypes = [C.c_char_p, i64, i64, P(d), P(i64), P(i32), P(d), P(d)]
         L.fim_read_tags.argtypes = [C.c_char_p, P(i64), P(i32)]
@@ -210,6 +223,27 @@ class Solver:
         s = FimStats()
         _check(lib().fim_get_stats(self.h, C.byref(s)), self.h)
         return {k: getattr(s, k) for k, _ in FimStats._fields_}
+
+    def autotune(self, stream=None):
+        """Times candidate launch configurations on the staged problem and keeps the fastest (dict)."""
+        t = FimTuneInfo()
+        _check(lib().fim_autotune(self.h, C.c_void_p(stream) if stream else None, C.byref(t)), self.h)
+        return {k: getattr(t, k) for k, _ in FimTuneInfo._fields_}
+
+    def tune_info(self):
+        t = FimTuneInfo()
+        _check(lib().fim_get_tune(self.h, C.byref(t)), self.h)
+        return {k: getattr(t, k) for k, _ in FimTuneInfo._fields_}
+
+    def set_tune(self, slots=None, corners=None, grid=None, dag_warps=None):
+        """Pins a launch configuration (all None: back to the default)."""
+        if slots is None and corners is None and grid is None and dag_warps is None:
+            _check(lib().fim_set_tune(self.h, None), self.h)
+            return
+        cur = self.tune_info()
+        t = FimTuneInfo(batch_slots=slots or cur["batch_slots"], batch_corners=corners or cur["batch_corners"],
+                        grid_blocks=grid or cur["grid_blocks"], dag_warps=dag_warps or cur["dag_warps"])
+        _check(lib().fim_set_tune(self.h, C.byref(t)), self.h)
 
     def features(self, d_features):
         """Writes the BF16 feature rows [n_vertices x MLP_INPUTS] to device memory; returns the time scale."""
@@ -333,6 +367,11 @@ class Batch:
         s = FimStats()
         _bcheck(lib().fim_batch_get_stats(self.h, C.byref(s)), self.h)
         return {k: getattr(s, k) for k, _ in FimStats._fields_}
+
+    def autotune(self, stream=None):
+        t = FimTuneInfo()
+        _bcheck(lib().fim_batch_autotune(self.h, C.c_void_p(stream) if stream else None, C.byref(t)), self.h)
+        return {k: getattr(t, k) for k, _ in FimTuneInfo._fields_}
 
 
 def solve_case(case, atags=None, **opts):

@@ -74,6 +74,8 @@ typedef struct {
   int exact_all;         /* 1: solve every triangle/tet candidate in FP64 instead of
                               screening them with FP32 interval bounds first; the
                               results are identical, only slower (cross-check)     */
+  int autotune;          /* 1: the first fim_solve after fim_set_mesh (or
+                              fim_batch_solve after an add) runs fim_autotune first */
 } fim_opts;
 
 /* Defaults: device 0, one endless window, reference front width, APD off. */
@@ -139,8 +141,40 @@ typedef struct {
   int64_t n_corners;       /* (vertex, tet) pairs of the mesh               */
   int grid_blocks;         /* persistent grid size of the FIM kernel        */
   int block_threads;
+  int batch_slots;         /* batch shape of the last solve: vertices ...   */
+  int batch_corners;       /* ... and corners a block stages at once        */
+  int dag_warps;           /* warps running FP64 tet prefixes per batch     */
 } fim_stats;
 int fim_get_stats(const fim_solver *s, fim_stats *out);
+
+/* Autotuner -- replaces the reference's external partition and fixed block
+ * size (extract_submeshes2, src/core/types.cpp:306-570; compute_step<<<nA,
+ * 256>>>, src/eikonal/cuda_fim.cu:2435).  Times full solves of the staged
+ * problem (mesh, conduction, stimuli set) under candidate launch
+ * configurations of the persistent kernel -- the batch shape (vertices x
+ * corners a block stages at once), the number of persistent blocks and the
+ * warps running the FP64 tet prefixes -- and keeps the fastest for every
+ * later solve of this mesh (fim_set_mesh forgets it).  Every configuration
+ * gives bit-identical times; the solver's last results are those of the
+ * last timed run.  info (or NULL) receives the choice. */
+typedef struct {
+  int batch_slots;      /* chosen batch shape: vertices ...                       */
+  int batch_corners;    /* ... and corners per batch                              */
+  int grid_blocks;      /* persistent blocks                                      */
+  int dag_warps;        /* warps running FP64 tet prefixes                        */
+  double default_ms;    /* solve time with the default configuration (0: untuned) */
+  double tuned_ms;      /* solve time with the chosen one                         */
+  int candidates;       /* configurations timed                                   */
+} fim_tune_info;
+int fim_autotune(fim_solver *s, void *stream, fim_tune_info *info);
+/* The configuration in use (the default one until tuned). */
+int fim_get_tune(const fim_solver *s, fim_tune_info *info);
+/* Pins a configuration (e.g. one fim_autotune chose in an earlier run):
+ * batch_slots/batch_corners must name a compiled batch shape (192x4096,
+ * 160x3072, 96x2048), grid_blocks lie in [1, the shape's co-resident grid],
+ * dag_warps in [1, 12]; the timing fields are ignored.  NULL restores the
+ * default configuration. */
+int fim_set_tune(fim_solver *s, const fim_tune_info *cfg);
 
 /* Allocation-free re-solve -- no counterpart in the reference.
  * Solves s's mesh and conduction for the stimuli given here (host arrays,
@@ -195,6 +229,10 @@ int fim_batch_solve(fim_batch *b, void *stream);
 int fim_batch_get_times(fim_batch *b, int64_t problem, double *phi, int32_t *state);
 /* Statistics of the last batch solve (all problems together). */
 int fim_batch_get_stats(const fim_batch *b, fim_stats *out);
+/* Stages the batch if needed and runs fim_autotune on it (all problems in
+ * one launch, as fim_batch_solve runs them); results are then those of the
+ * batch's last timed solve. */
+int fim_batch_autotune(fim_batch *b, void *stream, fim_tune_info *info);
 
 /* Learned warm start -- no counterpart in the reference.
  * A per-vertex MLP (features -> 128 -> 128 -> 128 -> 1, ReLU; BF16 weights
