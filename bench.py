@@ -70,6 +70,7 @@ def parse_args():
                     help="batch workload: meshes,solves,min vertices,max vertices")
     ap.add_argument("--cells", type=str, default=None, help="override slab cells, e.g. 66,23,10")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default launch configuration")
     ap.add_argument("--e2e-steps", type=int, default=None)
     return ap.parse_args()
 
@@ -242,6 +243,8 @@ def run_mine(args):
     cf = torch.tensor(case["cf"], dtype=torch.float64, device=dev)
     ct = torch.tensor(case["ct"], dtype=torch.float64, device=dev)
     s.set_stimuli(case["seed_v"], case["seed_t"])
+    s.set_conduction_device(fib.data_ptr(), cf.data_ptr(), ct.data_ptr())
+    tune = s.autotune() if not args.no_autotune else s.tune_info()  # before the timed region
     torch.cuda.synchronize()
 
     solve_ms, metric_ms = [], []
@@ -331,6 +334,11 @@ def run_mine(args):
                 "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": (metric_launches(nT) + 1) * args.steps,
         "clocks": clk,
+        "autotune": {"batch_vertices": tune["batch_slots"], "batch_corners": tune["batch_corners"],
+                     "grid_blocks": tune["grid_blocks"], "fp64_tet_warps": tune["dag_warps"],
+                     "default_ms": tune["default_ms"], "tuned_ms": tune["tuned_ms"],
+                     "gain_vs_default": (tune["default_ms"] / tune["tuned_ms"]) if tune["tuned_ms"] else None,
+                     "candidates": tune["candidates"]},
     }
     if world == 1 and not args.no_cpu_baseline:
         phi_o, _, ost = oracle_solve(case)
@@ -401,6 +409,7 @@ def run_batch(args):
     b = fim_api.Batch()
     for p in probs:
         b.add(p["xyz"], p["tets"], p["fib"], p["cf"], p["ct"], p["seed_v"], p["seed_t"])
+    tune = b.autotune() if not args.no_autotune else None
     for _ in range(max(args.warmup, 0)):
         b.solve()
     clocks = ClockSampler(index=0)
@@ -438,6 +447,7 @@ def run_batch(args):
                 "d2h_bytes_per_step": int(12 * cfg["vertices_total"]),
                 "how": "wall time of fim_batch_solve (launch + D2H of every problem's times and states)"},
         "gpu_launches": args.steps, "clocks": clk,
+        "autotune": tune,
     }
     if not args.no_cpu_baseline:
         from oracle import oracle as O

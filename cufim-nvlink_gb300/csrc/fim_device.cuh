@@ -311,4 +311,17 @@ static __device__ bool grid_sync(FimCtl *ctl, uint32_t nblocks, uint64_t timeout
   return s_ok != 0;
 }
 
+// Order-preserving map of doubles to unsigned integers, so that the minimum
+// of a vertex's candidates can be formed with integer atomicMin.
+__device__ __forceinline__ unsigned long long dkey(double x)
+{
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double dunkey(unsigned long long k)
+{
+  const unsigned long long b = (k >> 63) ? (k & 0x7fffffffffffffffull) : ~k;
+  return __longlong_as_double((long long)b);
+}
+
 }  // namespace fimgb

@@ -46,6 +46,9 @@ struct FimCtl {
   int64_t vertex_updates;
   int64_t corner_evals;
   int64_t exact_evals;
+  int32_t n_bad;                 // support check: reached times below every candidate bound
+  int32_t pad2;
+  unsigned long long tmin_key;   // dkey of the smallest such time
 };
 
 // Everything the persistent kernel touches, as device pointers.
@@ -107,6 +110,7 @@ struct FimParams {
   int32_t exact_all;       // 1: every local solve in FP64, no interval filter
   int32_t two_phase;       // 1: two grid-synchronised phases per iteration (endless window only)
   int32_t dag_warps;       // warps running the FP64 tet prefix groups of a batch (1..kDagWarpsMax)
+  int32_t resume;          // 1: keep the times and states as they are (no reset, no seeding)
 };
 
 // Most warps of a batch that run FP64 tet prefix groups (the scratch is
@@ -139,6 +143,16 @@ cudaError_t solve_prepare(int shape, int device, int block, int *max_grid);
 cudaError_t launch_solve(const FimDev &d, const FimParams &p, int shape, int grid, int block, cudaStream_t stream);
 // Writes phi (any order) into out.
 cudaError_t launch_copy(const double *src, double *dst, int64_t n, cudaStream_t stream);
+// Support check of a finished solve (fim_kernels.cu): every reached vertex
+// that is not a seed (is_seed[v] == 0) and whose time lies below a rigorous
+// lower bound of every candidate of its neighbours counts into ctl->n_bad
+// and lowers ctl->tmin_key to its time.
+cudaError_t launch_support_check(const FimDev &d, double lower, const uint8_t *is_seed, cudaStream_t stream);
+// Marks the seeds of d in is_seed (after the caller cleared it).
+cudaError_t launch_mark_seeds(const FimDev &d, uint8_t *is_seed, cudaStream_t stream);
+// Resets every vertex with a time >= tmin to INF / far, lists every other
+// reached vertex as narrow, then re-seeds the stimuli (two launches).
+cudaError_t launch_warm_reset(const FimDev &d, double tmin, cudaStream_t stream);
 
 // ---- learned warm start (fim_mlp.cu) ----
 // Network 7 (padded to kMlpIn) -> kMlpH -> kMlpH -> kMlpH -> 1.  Parameter

@@ -24,6 +24,8 @@
 //    phases per iteration with windows, two with one endless window.
 #include "fim_device.cuh"
 
+#include <cmath>
+
 namespace fimgb {
 
 // ---------------------------------------------------------------------------
@@ -182,6 +184,138 @@ cudaError_t launch_solve(const FimDev &d, const FimParams &p, int shape, int gri
     case 2: return solve_launch_s96(d, p, grid, block, stream);
     default: return cudaErrorInvalidValue;
   }
+}
+
+// ---------------------------------------------------------------------------
+// support check of a warm-started solve
+//
+// FIM only lowers times, so a start below the true time of a vertex would
+// stay there.  Such a time is not attained by any candidate its neighbours
+// can give: the reference's edge, triangle and tet updates
+// (update_per_element, cuda_fim.h:1362-1411) all return at least the
+// smallest time involved plus a distance.  The check bounds every candidate
+// of every corner from below with the same rigorous FP32 bounds the screens
+// use (edge: time + length; triangle pairs and tet: smallest time +
+// root-term bound, solve_lo) and flags a reached, non-seed vertex whose
+// time is strictly below all of them.  A cold solve never trips it: each of
+// its times was a candidate when it was set, and neighbour times only fall
+// afterwards, which only lowers the bounds.
+
+__global__ void fim_support_kernel(FimDev d, double lower, float lower_lo, float lower_hi,
+                                   const uint8_t *__restrict__ is_seed)
+{
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < d.nV; v += stride) {
+    const double pv = __ldcg(d.phi + v);
+    if (!(pv < FIM_INF) || is_seed[v]) continue;
+    float L = INFINITY;
+    for (int64_t c = d.cptr[v]; c < d.cptr[v + 1]; ++c) {
+      const uint4 h0 = __ldg(d.crec + kCrecWords * c), h1 = __ldg(d.crec + kCrecWords * c + 1);
+      const int32_t nb[3] = {(int32_t)h0.x, (int32_t)h0.y, (int32_t)h0.z};
+      const float len[3] = {__uint_as_float(h1.x), __uint_as_float(h1.y), __uint_as_float(h1.z)};
+      float lo[3], hi[3];
+      bool ok[3];
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        const Re P = re_in(__ldcg(d.phi_f + nb[i]));
+        bool valid = (__ldcg(d.sw + nb[i]) & 0xffu) >= ST_NARROW;
+        if (valid) {
+          if (re_lo(P) > lower_hi) valid = true;
+          else if (re_hi(P) <= lower_lo) valid = false;
+          else valid = __ldcg(d.phi + nb[i]) > lower;
+        }
+        ok[i] = valid;
+        lo[i] = re_lo(P);
+        hi[i] = re_hi(P);
+        if (valid) L = fminf(L, re_lo(P + re_len(len[i])));
+      }
+      if (ok[0] && ok[1]) L = fminf(L, solve_lo(fminf(lo[0], lo[1]), fmaxf(hi[0], hi[1]), half_lo(h0.w)));
+      if (ok[1] && ok[2]) L = fminf(L, solve_lo(fminf(lo[1], lo[2]), fmaxf(hi[1], hi[2]), half_hi(h0.w)));
+      if (ok[0] && ok[2]) L = fminf(L, solve_lo(fminf(lo[0], lo[2]), fmaxf(hi[0], hi[2]), half_lo(h1.w)));
+      if (ok[0] && ok[1] && ok[2])
+        L = fminf(L, solve_lo(fminf(lo[0], fminf(lo[1], lo[2])), fmaxf(hi[0], fmaxf(hi[1], hi[2])), half_hi(h1.w)));
+    }
+    if ((double)L > pv) {
+      atomicAdd(&d.ctl->n_bad, 1);
+      atomicMin(&d.ctl->tmin_key, dkey(pv));
+    }
+  }
+}
+
+__global__ void fim_mark_seeds_kernel(const int32_t *__restrict__ seed_v, int32_t n, uint8_t *is_seed)
+{
+  for (int32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) is_seed[seed_v[i]] = 1;
+}
+
+__global__ void fim_warm_reset_kernel(FimDev d, double tmin)
+{
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < d.nV; v += stride) {
+    const double x = d.phi[v];
+    d.tst[v] = ST_FAR;
+    if (x >= tmin) {
+      d.phi[v] = FIM_INF; d.phi2[v] = FIM_INF;
+      d.phi_f[v] = (float)FIM_INF; d.phi2_f[v] = (float)FIM_INF;
+      d.sw[v] = ST_FAR;
+    } else if (x < FIM_INF) {
+      d.sw[v] = ST_NARROW;
+    }
+  }
+}
+
+__global__ void fim_reseed_kernel(FimDev d)
+{
+  for (int32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < d.nseed; i += gridDim.x * blockDim.x) {
+    const int32_t v = d.seed_v[i];
+    const double x = d.seed_t[i];
+    d.phi[v] = x; d.phi2[v] = x;
+    d.phi_f[v] = (float)x; d.phi2_f[v] = (float)x;
+    d.sw[v] = ST_NARROW;
+  }
+}
+
+// float bounds of a double (round down / up), on the host
+static float f_rd(double x)
+{
+  float f = (float)x;
+  if ((double)f > x) f = std::nextafter(f, -INFINITY);
+  return f;
+}
+static float f_ru(double x)
+{
+  float f = (float)x;
+  if ((double)f < x) f = std::nextafter(f, INFINITY);
+  return f;
+}
+
+static unsigned grid_for(int64_t n, int block, unsigned cap)
+{
+  int64_t g = (n + block - 1) / block;
+  if (g < 1) g = 1;
+  return (unsigned)(g > cap ? cap : g);
+}
+
+cudaError_t launch_support_check(const FimDev &d, double lower, const uint8_t *is_seed, cudaStream_t stream)
+{
+  fim_support_kernel<<<grid_for(d.nV, 256, 152 * 16), 256, 0, stream>>>(d, lower, f_rd(lower), f_ru(lower),
+                                                                        is_seed);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mark_seeds(const FimDev &d, uint8_t *is_seed, cudaStream_t stream)
+{
+  if (d.nseed <= 0) return cudaSuccess;
+  fim_mark_seeds_kernel<<<grid_for(d.nseed, 256, 152), 256, 0, stream>>>(d.seed_v, d.nseed, is_seed);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_warm_reset(const FimDev &d, double tmin, cudaStream_t stream)
+{
+  fim_warm_reset_kernel<<<grid_for(d.nV, 256, 152 * 16), 256, 0, stream>>>(d, tmin);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess || d.nseed <= 0) return e;
+  fim_reseed_kernel<<<grid_for(d.nseed, 256, 152), 256, 0, stream>>>(d);
+  return cudaGetLastError();
 }
 
 __global__ void fim_copy_kernel(const double *__restrict__ src, double *__restrict__ dst, int64_t n)

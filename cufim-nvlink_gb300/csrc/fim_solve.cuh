@@ -45,18 +45,6 @@ __device__ __forceinline__ void probe_count(const FimDev &d, int k)
 enum : int { kPrSetup = 0, kPrA, kPrB, kPrS, kPrD, kPrE, kPrMark, kPrBarrier, kPrLight, kPrBatches,
              kPrPhases };
 
-// Order-preserving map of doubles to unsigned integers, so that the minimum
-// of a vertex's candidates can be formed with integer atomicMin.
-__device__ __forceinline__ unsigned long long dkey(double x)
-{
-  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-  return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
-}
-__device__ __forceinline__ double dunkey(unsigned long long k)
-{
-  const unsigned long long b = (k >> 63) ? (k & 0x7fffffffffffffffull) : ~k;
-  return __longlong_as_double((long long)b);
-}
 
 // One block of 16 warps per SM: the FP64 solves of a batch are packed into
 // as few warps as possible, and those warps sit on different SM
@@ -898,20 +886,23 @@ __global__ void __launch_bounds__(kThreads, 1) fim_solve_kernel(FimDev d, FimPar
   PROBE(-1);
 
   // reset_states_gpu + update_events_gpu: phi = INF, far; seeds narrow.
-  // (warm start: every vertex narrow at its given time instead)
-  for (int64_t v = gtid; v < d.nV; v += nthreads) {
-    const double x = d.phi_init ? d.phi_init[v] : FIM_INF;
-    set_phi_both(d, v, x); d.sw[v] = x < FIM_INF ? ST_NARROW : ST_FAR; d.tst[v] = ST_FAR;
+  // (warm start: every vertex narrow at its given time instead; resume: the
+  // times and states as they are, the narrow ones listed below)
+  if (!p.resume) {
+    for (int64_t v = gtid; v < d.nV; v += nthreads) {
+      const double x = d.phi_init ? d.phi_init[v] : FIM_INF;
+      set_phi_both(d, v, x); d.sw[v] = x < FIM_INF ? ST_NARROW : ST_FAR; d.tst[v] = ST_FAR;
+    }
+    // failure-detection test hook: this block never arrives at the barrier (a
+    // flag that nothing sets), so the others' bounded waits must expire
+    if (p.withhold_block > 0 && (int64_t)blockIdx.x == (int64_t)p.withhold_block - 1) return;
+    if (!grid_sync_probed(d, nblocks, p.timeout_ns, ++where)) return;
+    for (int64_t i = gtid; i < d.nseed; i += nthreads) {
+      const int32_t v = d.seed_v[i];
+      set_phi_both(d, v, d.seed_t[i]); d.sw[v] = ST_NARROW;
+    }
+    if (!grid_sync_probed(d, nblocks, p.timeout_ns, ++where)) return;
   }
-  // failure-detection test hook: this block never arrives at the barrier (a
-  // flag that nothing sets), so the others' bounded waits must expire
-  if (p.withhold_block > 0 && (int64_t)blockIdx.x == (int64_t)p.withhold_block - 1) return;
-  if (!grid_sync_probed(d, nblocks, p.timeout_ns, ++where)) return;
-  for (int64_t i = gtid; i < d.nseed; i += nthreads) {
-    const int32_t v = d.seed_v[i];
-    set_phi_both(d, v, d.seed_t[i]); d.sw[v] = ST_NARROW;
-  }
-  if (!grid_sync_probed(d, nblocks, p.timeout_ns, ++where)) return;
 
   int64_t it = 0;  // global iteration counter (identical in every block)
   double cur_time = 0.0, phi_start = 0.0;

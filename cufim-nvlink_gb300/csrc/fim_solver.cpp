@@ -673,11 +673,12 @@ static void print_probe(fim_solver *s, int grid)
 #endif
 
 static int tune_solver(fim_solver *s, cudaStream_t st);
+static int warm_check(fim_solver *s, cudaStream_t st);
 
-// One solve with launch configuration (shape, grid, dag_warps).
-static int run_solve(fim_solver *s, cudaStream_t st, int shape, int grid, int dag_warps)
+// Launch parameters and device view of the solver's staged problem.
+static void solve_args(const fim_solver *s, FimDev &d, FimParams &p)
 {
-  FimDev d{};
+  d = FimDev{};
   d.nV = (int32_t)s->nL; d.nG = (int32_t)s->nV; d.nT = s->nT; d.nC = s->nC;
   d.gptr = s->gptr.p; d.gcopy = s->gcopy.p; d.phi_out = s->phi_out.p; d.st_out = s->st_out.p;
   d.cptr = s->cptr.p; d.crec = s->crec.p; d.cgeo = s->cgeo.p; d.cgf = s->cgf.p; d.nptr = s->nptr.p; d.nbr = s->nbr.p;
@@ -688,18 +689,28 @@ static int run_solve(fim_solver *s, cudaStream_t st, int shape, int grid, int da
   d.seed_v = s->seed_v.p; d.seed_t = s->seed_t.p; d.nseed = s->nseed;
   d.phi_init = s->warm;
   d.ctl = s->ctl.p;
-  FimParams p{};
+  p = FimParams{};
   p.dt = s->opts.dt;
   p.n_steps = s->opts.n_steps;
   p.front_width = s->opts.front_width >= 0.0 ? s->opts.front_width : s->front_width;
   p.apd = s->opts.apd;
   p.max_iter = s->opts.max_iterations > 0 ? s->opts.max_iterations : 10000000;
   p.timeout_ns = (uint64_t)(s->opts.timeout_s * 1e9);
-  p.withhold_block = (s->opts.test_withhold_block > 0 && s->opts.test_withhold_block <= grid)
-                         ? s->opts.test_withhold_block : 0;
   p.exact_all = s->opts.exact_all ? 1 : 0;
   p.two_phase = two_phase_ok(p) ? 1 : 0;
+}
+
+// One solve with launch configuration (shape, grid, dag_warps); resume keeps
+// the times and states in place instead of resetting and seeding them.
+static int run_solve(fim_solver *s, cudaStream_t st, int shape, int grid, int dag_warps, bool resume = false)
+{
+  FimDev d{};
+  FimParams p{};
+  solve_args(s, d, p);
+  p.withhold_block = (s->opts.test_withhold_block > 0 && s->opts.test_withhold_block <= grid)
+                         ? s->opts.test_withhold_block : 0;
   p.dag_warps = dag_warps;
+  p.resume = resume ? 1 : 0;
 #ifdef FIM_PROBE
   CUDA_TRY(s, s->probe.reserve((size_t)grid * kProbeSlots));
   CUDA_TRY(s, cudaMemsetAsync(s->probe.p, 0, sizeof(unsigned long long) * grid * kProbeSlots, st));
@@ -747,7 +758,86 @@ extern "C" int fim_solve(fim_solver *s, void *stream)
     const int rc = tune_solver(s, st);
     if (rc != FIM_OK) return rc;
   }
-  return run_solve(s, st, s->shape, s->grid, s->dag_warps);
+  int rc = run_solve(s, st, s->shape, s->grid, s->dag_warps);
+  s->stats.warm_reset = 0;
+  s->stats.warm_rounds = 0;
+  if (rc != FIM_OK || !s->warm || !(std::isinf(s->opts.dt) && s->opts.n_steps == 1)) return rc;
+  return warm_check(s, st);
+}
+
+// ---------------------------------------------------------------------------
+// support check of warm-started solves
+//
+// FIM only lowers times, so a start below the true time of a vertex would
+// stay wrong.  After a warm-started solve, fim_support_kernel flags every
+// reached non-seed vertex whose time lies below a rigorous lower bound of
+// every candidate of its neighbours (a cold solve never has one).  Such a
+// vertex, and every vertex downwind of it, has a time at least as large as
+// the smallest flagged time tmin, so all times >= tmin are reset to INF and
+// FIM resumes from the times below tmin (and the stimuli); the check then
+// runs again.  After kWarmRounds rounds that still find flagged vertices,
+// the solve is redone cold.
+constexpr int kWarmRounds = 3;
+
+static int warm_check(fim_solver *s, cudaStream_t st)
+{
+  FimDev d{};
+  FimParams p{};
+  solve_args(s, d, p);
+  const double lower = -p.front_width;
+  double total_ms = s->stats.solve_ms;
+  int64_t iters = s->stats.iterations, upd = s->stats.vertex_updates;
+  int64_t reset = 0;
+  int rounds = 0;
+  for (;;) {
+    float ms = 0.f;
+    CUDA_TRY(s, cudaEventRecord(s->ev0, st));
+    CUDA_TRY(s, cudaMemsetAsync(s->dec.p, 0, s->nL, st));
+    CUDA_TRY(s, launch_mark_seeds(d, s->dec.p, st));
+    CUDA_TRY(s, cudaMemsetAsync(&s->ctl.p->n_bad, 0, sizeof(int32_t), st));
+    CUDA_TRY(s, cudaMemsetAsync(&s->ctl.p->tmin_key, 0xff, sizeof(unsigned long long), st));
+    CUDA_TRY(s, launch_support_check(d, lower, s->dec.p, st));
+    CUDA_TRY(s, cudaEventRecord(s->ev1, st));
+    FimCtl h{};
+    CUDA_TRY(s, cudaMemcpyAsync(&h, s->ctl.p, sizeof(FimCtl), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(s, cudaStreamSynchronize(st));
+    cudaEventElapsedTime(&ms, s->ev0, s->ev1);
+    total_ms += ms;
+    if (h.n_bad == 0) break;
+    reset += h.n_bad;
+    int rc;
+    if (rounds == kWarmRounds) {  // give up on the start: a cold solve
+      const double *w = s->warm;
+      s->warm = nullptr;
+      rc = run_solve(s, st, s->shape, s->grid, s->dag_warps);
+      s->warm = w;
+      if (rc != FIM_OK) return rc;
+      total_ms += s->stats.solve_ms;
+      iters += s->stats.iterations;
+      upd += s->stats.vertex_updates;
+      ++rounds;
+      break;
+    }
+    const unsigned long long k = h.tmin_key;
+    const unsigned long long b = (k >> 63) ? (k & 0x7fffffffffffffffull) : ~k;
+    double tmin;
+    std::memcpy(&tmin, &b, sizeof tmin);
+    CUDA_TRY(s, cudaEventRecord(s->ev0, st));
+    CUDA_TRY(s, launch_warm_reset(d, tmin, st));
+    CUDA_TRY(s, cudaEventRecord(s->ev1, st));
+    if ((rc = run_solve(s, st, s->shape, s->grid, s->dag_warps, true)) != FIM_OK) return rc;
+    cudaEventElapsedTime(&ms, s->ev0, s->ev1);
+    total_ms += ms + s->stats.solve_ms;
+    iters += s->stats.iterations;
+    upd += s->stats.vertex_updates;
+    ++rounds;
+  }
+  s->stats.solve_ms = total_ms;
+  s->stats.iterations = iters;
+  s->stats.vertex_updates = upd;
+  s->stats.warm_reset = reset;
+  s->stats.warm_rounds = rounds;
+  return FIM_OK;
 }
 
 // ---------------------------------------------------------------------------

@@ -46,7 +46,8 @@ class FimStats(C.Structure):
     _fields_ = [("iterations", C.c_int64), ("vertex_updates", C.c_int64), ("corner_evals", C.c_int64),
                 ("exact_evals", C.c_int64), ("solve_ms", C.c_double), ("metric_ms", C.c_double), ("n_corners", C.c_int64),
                 ("grid_blocks", C.c_int), ("block_threads", C.c_int), ("batch_slots", C.c_int),
-                ("batch_corners", C.c_int), ("dag_warps", C.c_int)]
+                ("batch_corners", C.c_int), ("dag_warps", C.c_int), ("warm_reset", C.c_int64),
+                ("warm_rounds", C.c_int)]
 
 
 class FimTuneInfo(C.Structure):

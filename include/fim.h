@@ -144,6 +144,8 @@ typedef struct {
   int batch_slots;         /* batch shape of the last solve: vertices ...   */
   int batch_corners;       /* ... and corners a block stages at once        */
   int dag_warps;           /* warps running FP64 tet prefixes per batch     */
+  int64_t warm_reset;      /* warm start: times the support check rejected  */
+  int warm_rounds;         /* warm start: check-reset-resume rounds run     */
 } fim_stats;
 int fim_get_stats(const fim_solver *s, fim_stats *out);
 
@@ -272,8 +274,19 @@ int fim_mlp_predict(fim_mlp *m, int64_t n, const void *d_features, float *d_out)
 int fim_features(fim_solver *s, void *d_features, float *time_scale);
 /* Start times (device, FP64 [n_vertices], complete before and kept by the
  * caller until the solve) for the next solves; NULL restores the cold start.
- * FIM only lowers times, so a start below the true time of a vertex stays
- * wrong, and a start below the earliest stimulus time can keep the
+ * FIM only lowers times, so a start below the true time of a vertex would
+ * stay wrong.  With one endless window every warm-started fim_solve
+ * therefore ends with a support check: a reached vertex (not a stimulus)
+ * whose time lies below a rigorous lower bound of every candidate its
+ * neighbours give -- the reference's edge, triangle and tet updates all
+ * return at least their smallest input time plus a distance, and a cold
+ * solve never violates this -- marks its time tmin; every time >= tmin
+ * (the flagged vertices and everything downwind of them) is reset to INF and
+ * FIM resumes from the rest and the stimuli; the check repeats, and after 3
+ * rounds that still flag vertices the solve is redone cold.  fim_stats
+ * reports the rejected times (warm_reset) and rounds; solve_ms and the
+ * counts cover all rounds.  A start only slightly below the truth can pass
+ * the check.  A start below the earliest stimulus time can keep the
  * iteration from settling (it then stops at max_iterations). */
 int fim_set_warm_start(fim_solver *s, const double *d_phi_init);
 

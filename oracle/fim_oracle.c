@@ -667,6 +667,36 @@ static double mesh_vertex_update(const orc_mesh *M, const double *phi, const int
   return nw;
 }
 
+/* Local support of a finished solve: U[v] = the minimum over every corner
+ * of v of the reference's local update (update_per_element,
+ * cuda_fim.h:1362-1411) from the final times and states of its neighbours,
+ * not counting v's own time (INF where no corner gives a value).  A time
+ * below its U is not attained by any candidate from its neighbours. */
+void orc_support(int nV, int64_t nT, const int32_t *tet_slots, const double *geo_slots, const double *phi,
+                 const int32_t *state, int tri_f32, double *U)
+{
+  orc_mesh M;
+  orc_mesh_build(&M, nV, nT, tet_slots, geo_slots);
+  #pragma omp parallel for schedule(dynamic, 256)
+  for (int v = 0; v < nV; ++v) {
+    double nw = ORC_INF;
+    for (int64_t k = M.n2e_ptr[v]; k < M.n2e_ptr[v + 1]; ++k) {
+      const int32_t e = M.n2e[k];
+      double ph[4]; int t = 0;
+      for (int s = 0; s < 4; ++s) {
+        const int32_t n = M.tv[4 * (int64_t)e + s];
+        if (n == v) { t = s; ph[s] = 0.0; }
+        else if (state[n] >= ST_NARROW) ph[s] = phi[n];
+        else ph[s] = ORC_INF;
+      }
+      const double c = orc_corner_update(M.geo + 6 * (int64_t)e, t, ph, tri_f32);
+      if (c < nw) nw = c;
+    }
+    U[v] = nw;
+  }
+  orc_mesh_free(&M);
+}
+
 long orc_solve_pure(int nV, int64_t nT, const int32_t *tet_slots, const double *geo_slots,
                     int nseed, const int32_t *seed_v, const double *seed_t, int tri_f32,
                     int threads, long max_iter, double *phi, int32_t *state_out, long *n_updates)

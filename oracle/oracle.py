@@ -49,6 +49,8 @@ def lib():
                                       C.c_int, C.c_long, P(d), P(d)]
         L.orc_front_width.restype = d
         L.orc_front_width.argtypes = [i64, P(i32), P(d), d]
+        L.orc_support.argtypes = [C.c_int, i64, P(i32), P(d), P(d), P(i32), C.c_int, P(d)]
+        L.orc_support.restype = None
         _lib = L
     return _lib
 
@@ -186,3 +188,16 @@ def ref_lib():
         L.ref_load_plan.argtypes = [C.c_char_p, C.c_char_p, P(d), P(i64), P(i64), P(i64), P(i64), P(d), P(d)]
         _ref = L
     return _ref
+
+
+def support(nV, tet_slots, geo_slots, phi, state, tri_f32=True):
+    """Per vertex, the minimum local update from its neighbours' final times
+    (orc_support): a reached time below it is unsupported."""
+    ts = np.ascontiguousarray(tet_slots, dtype=np.int32)
+    g = np.ascontiguousarray(geo_slots, dtype=np.float64)
+    ph = np.ascontiguousarray(phi, dtype=np.float64)
+    st = np.ascontiguousarray(state, dtype=np.int32)
+    U = np.empty(nV)
+    lib().orc_support(nV, ts.shape[0], _p(ts, C.c_int32), _p(g, C.c_double), _p(ph, C.c_double),
+                      _p(st, C.c_int32), 1 if tri_f32 else 0, _p(U, C.c_double))
+    return U

@@ -80,6 +80,7 @@ def test_warm_start_bit_exact(F, O):
         s.solve()
         phi, st = s.times()
         it = s.stats()["iterations"]
+        assert s.stats()["warm_reset"] == 0 and s.stats()["warm_rounds"] == 0  # an upper bound passes the check
     slots, _, _, _ = O.reference_slots(nV, c["tets"], None)
     geo = O.metric_geo(slots, c["xyz"], c["fib"], c["cf"], c["ct"])
     sv = np.concatenate([np.arange(nV), c["seed_v"]])
@@ -88,6 +89,42 @@ def test_warm_start_bit_exact(F, O):
     phi_o, st_o, it_o, _ = O.solve_pure(nV, slots, geo, sv[keep], st0[keep])
     assert_identical(phi, st, phi_o, st_o)
     assert it == it_o
+
+
+@pytest.mark.parametrize("scale", [0.5, 0.9])
+def test_warm_start_below_truth_is_reset(F, O, scale):
+    """A start below the true times in the middle third of the slab (the rest
+    1.05 x the cold result): the support check must flag it, reset it with
+    everything downwind and resume, so that no time ends far below the cold
+    solve; without the check the region would keep scale x its true times."""
+    import fim_mesh
+    torch = pytest.importorskip("torch")
+    c = fim_mesh.slab_case(cells=(40, 14, 6), size=(20.0, 7.0, 3.0), seed=5)
+    cold, _, _ = F.solve_case(c)
+    x = c["xyz"][:, 0]
+    mid = (x > 20.0 / 3) & (x < 40.0 / 3)
+    reached = cold < F.INF
+    start = np.where(reached, np.where(mid, scale, 1.05) * cold, F.INF)
+    d_start = torch.from_numpy(start).cuda()
+    torch.cuda.synchronize()
+    with F.Solver() as s:
+        s.set_mesh(c["xyz"], c["tets"])
+        s.set_conduction(c["fib"], c["cf"], c["ct"])
+        s.set_stimuli(c["seed_v"], c["seed_t"])
+        s.set_warm_start(d_start.data_ptr())
+        s.solve()
+        phi, _ = s.times()
+        stt = s.stats()
+        s.set_warm_start(None)
+        s.solve()
+        again, _ = s.times()
+    assert np.array_equal(again, cold)  # the cold start is back
+    assert stt["warm_reset"] > 0 and stt["warm_rounds"] >= 1
+    tmax = cold[reached].max()
+    assert np.array_equal(phi < F.INF, reached)
+    below = (cold - phi)[reached] / tmax
+    assert below.max() < 1e-2, f"a time ends {below.max():.3g} x max(t) below the cold solve"
+    assert np.abs(phi - cold)[reached].max() / tmax < 2e-2
 
 
 def _ut(O, tag_key):
