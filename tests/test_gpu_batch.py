@@ -68,3 +68,33 @@ def test_batch_rejects_windows_and_negative_times(F):
         assert e.value.code == 1 and "times >= 0" in str(e.value)
         with pytest.raises(F.FimError):
             b.solve()  # nothing added
+
+
+def test_wide_batch_every_problem(F, O):
+    """34 problems in one launch: 32 uneven boxes with 1-8 stimuli, a
+    112,716-vertex anisotropic slab and a single-stimulus cube.  Every problem
+    equals its own single solve bit for bit; four (the slab, the cube and
+    the two smallest boxes) also equal the FP64 oracle."""
+    import fim_mesh
+    probs = _problems(n_meshes=12, n_solves=32, vmin=300, vmax=20000, seed=23)
+    big = fim_mesh.slab_case(cells=(100, 35, 30), size=(20.0, 7.0, 3.0), seed=13)
+    one = fim_mesh.cube_case(10, seed=4)
+    assert len(one["seed_v"]) == 1 and big["xyz"].shape[0] > 100_000
+    probs = probs + [{k: big[k] for k in ("xyz", "tets", "fib", "cf", "ct", "seed_v", "seed_t")},
+                     {k: one[k] for k in ("xyz", "tets", "fib", "cf", "ct", "seed_v", "seed_t")}]
+    with F.Batch() as b:
+        ids = [b.add(p["xyz"], p["tets"], p["fib"], p["cf"], p["ct"], p["seed_v"], p["seed_t"]) for p in probs]
+        b.solve()
+        got = [b.times(i) for i in ids]
+    for k, (p, (phi, st)) in enumerate(zip(probs, got)):
+        phi1, st1, _ = F.solve_case(p)
+        assert np.array_equal(phi, phi1) and np.array_equal(st, st1), f"problem {k} differs from its single solve"
+    order = sorted(range(32), key=lambda i: probs[i]["xyz"].shape[0])
+    for k in [32, 33] + order[:2]:
+        p = probs[k]
+        phi, st = got[k]
+        nV = p["xyz"].shape[0]
+        slots, _, _, _ = O.reference_slots(nV, p["tets"], None)
+        geo = O.metric_geo(slots, p["xyz"], p["fib"], p["cf"], p["ct"])
+        phi_o, st_o, _, _ = O.solve_pure(nV, slots, geo, p["seed_v"], p["seed_t"])
+        assert np.array_equal(phi, phi_o) and np.array_equal(st, st_o), f"problem {k} differs from the oracle"
