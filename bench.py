@@ -476,50 +476,90 @@ def run_batch(args):
 
 def run_warm(args):
     """Trains the warm-start network on FIM maps of small slabs of the bench
-    family (generated by the solver), then solves held-out maps cold and warm.
-    One step = one held-out map solved once each way."""
+    family (generated by the solver), then solves held-out maps: one at a time
+    cold (the plain cold-start GPU FIM), cold in one batched launch, and warm
+    in one batched launch (start = 1.05 x the prediction, support-checked).
+    Errors are reported against the cold solves and against the oracle's
+    fixed point of the local solver (the truth a warm start approaches)."""
     import torch
     import fim_api
     import fim_warm
+    from oracle import build as obuild
+    from oracle import oracle as O
+    obuild.build_oracle()
     torch.cuda.set_device(0)
     cells = (66, 23, 10)
+    n_test = max(args.steps, 32)
     t0 = time.perf_counter()
     train_maps = fim_warm.make_maps(400, cells, 7, torch)
     gen_s = time.perf_counter() - t0
-    test_maps = fim_warm.make_maps(max(args.steps, 1), cells, 8, torch)
+    test_maps = fim_warm.make_maps(n_test, cells, 8, torch)
     mlp = fim_api.Mlp(seed=5)
     t0 = time.perf_counter()
     losses = fim_warm.train(mlp, train_maps, steps=3000, batch=4096, lr=1e-3, torch=torch)
     train_s = time.perf_counter() - t0
     ev = fim_warm.evaluate(mlp, test_maps, torch)
-    cold_ms, warm_ms, cold_it, warm_it, err, below = [], [], [], [], [], []
-    with fim_api.Solver() as s:
-        for m in test_maps:
-            phi, st, start = fim_warm.warm_solve(s, mlp, m, torch)
-            r = m.phi < 1e300
-            tmax = m.phi[r].max()
-            cold_ms.append(m.cold["solve_ms"])
-            warm_ms.append(st["solve_ms"])
-            cold_it.append(m.cold["iterations"])
-            warm_it.append(st["iterations"])
-            err.append(float(np.abs(phi - m.phi)[r].max() / tmax))
-            below.append(float(np.mean(start[r] < m.phi[r])))
+    cold_single_ms = float(sum(m.cold["solve_ms"] for m in test_maps))
+    starts = [torch.clamp(fim_warm.predict_times(mlp, m, torch) * 1.05, min=float(np.min(m.case["seed_t"])))
+              for m in test_maps]
+    d_start = torch.cat(starts).contiguous()
+    torch.cuda.synchronize()
+    b = fim_api.Batch()
+    for m in test_maps:
+        c = m.case
+        b.add(c["xyz"], c["tets"], c["fib"], c["cf"], c["ct"], c["seed_v"], c["seed_t"])
+    b.autotune()
+    clocks = ClockSampler(index=0)
+    clocks.start()
+    cold_b, warm_b = [], []
+    for _ in range(3):
+        b.set_warm_start(None)
+        b.solve()
+        cold_b.append(b.stats()["solve_ms"])
+        b.set_warm_start(d_start.data_ptr())
+        b.solve()
+        warm_b.append(b.stats()["solve_ms"])
+    clk = clocks.stop()
+    st_w = b.stats()
+    err_cold, err_fp, below_fp = [], [], []
+    for i, m in enumerate(test_maps):
+        phi = b.times(i, with_state=False)
+        c = m.case
+        r = m.phi < 1e300
+        tmax = m.phi[r].max()
+        slots, _, _, _ = O.reference_slots(m.nV, c["tets"], None)
+        geo = O.metric_geo(slots, c["xyz"], c["fib"], c["cf"], c["ct"])
+        fp, _ = O.fixed_point(m.nV, slots, geo, c["seed_v"], c["seed_t"])
+        err_cold.append(np.abs(phi - m.phi)[r] / tmax)
+        err_fp.append(np.abs(phi - fp)[r] / tmax)
+        below_fp.append(np.max((fp - phi)[r]) / tmax)
+    b.close()
     mlp.close()
+    ec, ef = np.concatenate(err_cold), np.concatenate(err_fp)
+    cold_single = n_test / (cold_single_ms * 1e-3)
+    cold_batched = n_test / (min(cold_b) * 1e-3)
+    warm_batched = n_test / (min(warm_b) * 1e-3)
     nv = test_maps[0].nV
     out = {
-        "metric": METRICS["warm"], "value": len(warm_ms) / (sum(warm_ms) * 1e-3), "unit": UNIT, "n_gpus": 1,
-        "steps": len(warm_ms), "warmup": 0, "ms_per_step": float(np.mean(warm_ms)), "higher_is_better": True,
+        "metric": METRICS["warm"], "value": warm_batched, "unit": UNIT, "n_gpus": 1,
+        "steps": 3, "warmup": 0, "ms_per_step": min(warm_b), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64 solve, bf16 network",
         "data": "synthetic (FIM maps of seeded slabs generated by the solver)",
-        "config": {"workload": (f"slab family {cells[0]}x{cells[1]}x{cells[2]} Kuhn cells ({nv} vertices), random "
-                                "cf/ct/fibre/scar/stimuli; network 7->128->128->128->1 trained on 400 maps, 3000 "
-                                "Adam steps of 4096 vertices; start = 1.05 x prediction"), "train_maps": 400},
-        "cold": {"value": len(cold_ms) / (sum(cold_ms) * 1e-3), "unit": UNIT, "iterations": float(np.mean(cold_it))},
-        "warm_iterations": float(np.mean(warm_it)),
-        "speedup_vs_cold": sum(cold_ms) / sum(warm_ms),
-        "warm_max_rel_err_vs_cold": max(err), "start_below_cold_frac": float(np.mean(below)),
+        "config": {"workload": (f"{n_test} held-out slabs {cells[0]}x{cells[1]}x{cells[2]} Kuhn cells ({nv} vertices), "
+                                "random cf/ct/fibre/scar/stimuli, solved in one batched launch from the learned start; "
+                                "network 7->128->128->128->1 trained on 400 maps, 3000 Adam steps of 4096 vertices; "
+                                "start = 1.05 x prediction"), "train_maps": 400, "test_maps": n_test},
+        "north_star_ratio": {"value": warm_batched / cold_single,
+                             "how": "warm-started batched solves/s / plain cold-start single-solve GPU FIM solves/s",
+                             "cold_batched_over_cold_single": cold_batched / cold_single,
+                             "warm_batched_over_cold_batched": warm_batched / cold_batched},
+        "cold_single": {"value": cold_single, "unit": UNIT}, "cold_batched": {"value": cold_batched, "unit": UNIT},
+        "warm_support_check": {"reset": st_w["warm_reset"], "rounds": st_w["warm_rounds"]},
+        "warm_err_vs_cold": {"max_rel": float(ec.max()), "rms_rel": float(np.sqrt(np.mean(ec ** 2)))},
+        "warm_err_vs_fixed_point": {"max_rel": float(ef.max()), "rms_rel": float(np.sqrt(np.mean(ef ** 2))),
+                                    "max_below_rel": float(max(below_fp))},
         "network": ev, "train_loss_first_last": [float(np.mean(losses[:10])), float(np.mean(losses[-50:]))],
-        "generation_s": gen_s, "training_s": train_s, "gpu_launches": 2 * len(warm_ms),
+        "generation_s": gen_s, "training_s": train_s, "gpu_launches": 6, "clocks": clk,
         "e2e": {"value": None, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0,
                 "how": "report line; the end-to-end number is the slab workload's"},
     }

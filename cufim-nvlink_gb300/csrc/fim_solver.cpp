@@ -1236,6 +1236,21 @@ extern "C" int fim_batch_autotune(fim_batch *b, void *stream, fim_tune_info *inf
   return FIM_OK;
 }
 
+extern "C" int fim_batch_set_warm_start(fim_batch *b, const double *d_phi_init)
+{
+  if (!b) return batch_err(nullptr, FIM_ERR_INVALID_ARGUMENT, "fim_batch_set_warm_start: batch is NULL");
+  if (d_phi_init && b->probs.empty())
+    return batch_err(b, FIM_ERR_NOT_READY, "fim_batch_set_warm_start: no problems added");
+  if (d_phi_init) {
+    const int rc = batch_stage(b, "fim_batch_set_warm_start");
+    if (rc != FIM_OK) return rc;
+  }
+  const int rc = fim_set_warm_start(b->s, d_phi_init);
+  if (rc != FIM_OK) return batch_err(b, rc, "fim_batch_set_warm_start: %s", fim_last_error(b->s));
+  b->solved = false;
+  return FIM_OK;
+}
+
 extern "C" int fim_batch_solve(fim_batch *b, void *stream)
 {
   if (!b) return batch_err(nullptr, FIM_ERR_INVALID_ARGUMENT, "fim_batch_solve: batch is NULL");

@@ -30,7 +30,7 @@ EXPORTS = ["fim_default_opts", "fim_create", "fim_destroy", "fim_last_error", "f
            "fim_batch_destroy", "fim_batch_last_error", "fim_batch_add", "fim_batch_solve", "fim_batch_get_times",
            "fim_batch_get_stats", "fim_mlp_create", "fim_mlp_destroy", "fim_mlp_set_params", "fim_mlp_get_params",
            "fim_mlp_gradients", "fim_mlp_train_step", "fim_mlp_predict", "fim_features", "fim_set_warm_start",
-           "fim_autotune", "fim_get_tune", "fim_set_tune", "fim_batch_autotune"]
+           "fim_autotune", "fim_get_tune", "fim_set_tune", "fim_batch_autotune", "fim_batch_set_warm_start"]
 MLP_INPUTS = 64
 MLP_PARAMS = 41473
 
@@ -117,6 +117,7 @@ def lib():
         L.fim_get_tune.argtypes = [vp, P(FimTuneInfo)]
         L.fim_set_tune.argtypes = [vp, P(FimTuneInfo)]
         L.fim_batch_autotune.argtypes = [vp, vp, P(FimTuneInfo)]
+        L.fim_batch_set_warm_start.argtypes = [vp, vp]
         L.fim_vtk_read.argtypes = [C.c_char_p, P(i64), P(i64), P(d), P(i64), P(i32)]
         L.fim_vtk_write.argtypes = [C.c_char_p, i64, i64, P(d), P(i64), P(i32), P(d), P(d)]
         L.fim_read_tags.argtypes = [C.c_char_p, P(i64), P(i32)]
@@ -373,6 +374,10 @@ class Batch:
         t = FimTuneInfo()
         _bcheck(lib().fim_batch_autotune(self.h, C.c_void_p(stream) if stream else None, C.byref(t)), self.h)
         return {k: getattr(t, k) for k, _ in FimTuneInfo._fields_}
+
+    def set_warm_start(self, d_phi):
+        """Start times of all problems' vertices (device FP64, in add order); None: cold."""
+        _bcheck(lib().fim_batch_set_warm_start(self.h, C.c_void_p(d_phi) if d_phi else None), self.h)
 
 
 def solve_case(case, atags=None, **opts):

@@ -235,6 +235,11 @@ int fim_batch_get_stats(const fim_batch *b, fim_stats *out);
  * one launch, as fim_batch_solve runs them); results are then those of the
  * batch's last timed solve. */
 int fim_batch_autotune(fim_batch *b, void *stream, fim_tune_info *info);
+/* Warm start of every problem at once: d_phi_init (device, FP64) holds the
+ * start times of all problems' vertices in the order they were added (as
+ * fim_set_warm_start; the support check runs over the whole batch); NULL
+ * restores the cold start.  Stages the batch if needed. */
+int fim_batch_set_warm_start(fim_batch *b, const double *d_phi_init);
 
 /* Learned warm start -- no counterpart in the reference.
  * A per-vertex MLP (features -> 128 -> 128 -> 128 -> 1, ReLU; BF16 weights

@@ -98,3 +98,38 @@ def test_wide_batch_every_problem(F, O):
         geo = O.metric_geo(slots, p["xyz"], p["fib"], p["cf"], p["ct"])
         phi_o, st_o, _, _ = O.solve_pure(nV, slots, geo, p["seed_v"], p["seed_t"])
         assert np.array_equal(phi, phi_o) and np.array_equal(st, st_o), f"problem {k} differs from the oracle"
+
+
+def test_batch_warm_start_equals_single_warm_solves(F):
+    """fim_batch_set_warm_start: upper-bound starts (1.05 x the cold times)
+    for three problems in one array, in add order; each problem's result
+    equals its own warm-started single solve bit for bit."""
+    import fim_mesh
+    torch = pytest.importorskip("torch")
+    cases = [fim_mesh.cube_case(n, seed=2 + n) for n in (6, 9, 7)]
+    starts, singles = [], []
+    for c in cases:
+        cold, _, _ = F.solve_case(c)
+        st = np.where(cold < F.INF, 1.05 * cold, F.INF)
+        starts.append(st)
+        d = torch.from_numpy(st).cuda()
+        torch.cuda.synchronize()
+        with F.Solver() as s:
+            s.set_mesh(c["xyz"], c["tets"])
+            s.set_conduction(c["fib"], c["cf"], c["ct"])
+            s.set_stimuli(c["seed_v"], c["seed_t"])
+            s.set_warm_start(d.data_ptr())
+            s.solve()
+            singles.append(s.times())
+            assert s.stats()["warm_reset"] == 0
+    d_all = torch.from_numpy(np.concatenate(starts)).cuda()
+    torch.cuda.synchronize()
+    with F.Batch() as b:
+        for c in cases:
+            b.add(c["xyz"], c["tets"], c["fib"], c["cf"], c["ct"], c["seed_v"], c["seed_t"])
+        b.set_warm_start(d_all.data_ptr())
+        b.solve()
+        assert b.stats()["warm_reset"] == 0
+        for i, (phi1, st1) in enumerate(singles):
+            phi, st = b.times(i)
+            assert np.array_equal(phi, phi1) and np.array_equal(st, st1)
