@@ -71,6 +71,9 @@ def parse_args():
     ap.add_argument("--cells", type=str, default=None, help="override slab cells, e.g. 66,23,10")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch configuration")
+    ap.add_argument("--precision", choices=["fp64", "fp32"], default="fp64",
+                    help="fp32: FP32 local solves wherever their screens are conclusive (not bit-exact; the "
+                         "parity block reports the error against the FP64 oracle)")
     ap.add_argument("--e2e-steps", type=int, default=None)
     return ap.parse_args()
 
@@ -209,7 +212,7 @@ def oracle_solve(case, threads=0):
     return phi, st, {"solve_s": t2 - t1, "prep_s": t1 - t0, "iterations": it, "vertex_updates": upd}
 
 
-def parity_report(phi, phi_o):
+def parity_report(phi, phi_o, tolerance="max |dt| <= 1e-4 max(t); achieved bit-exact"):
     finite = phi_o < 1e300
     tmax = float(phi_o[finite].max()) if finite.any() else 1.0
     d = np.abs(np.where(finite, phi, 0.0) - np.where(finite, phi_o, 0.0))
@@ -217,7 +220,7 @@ def parity_report(phi, phi_o):
     return {"max_abs_err": float(d.max()), "max_rel_err": float(d.max() / tmax),
             "rms_rel_err": float(np.sqrt(np.mean(d ** 2)) / tmax),
             "n_bit_mismatch": int(np.count_nonzero(phi != phi_o)), "unreached_match": same_inf,
-            "tolerance": "max |dt| <= 1e-4 max(t); achieved bit-exact"}
+            "tolerance": tolerance}
 
 
 def run_mine(args):
@@ -235,7 +238,7 @@ def run_mine(args):
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
 
-    s = fim_api.Solver(device=local)
+    s = fim_api.Solver(device=local, fp32_update=1 if args.precision == "fp32" else 0)
     s.set_mesh(case["xyz"], case["tets"])
     stream = torch.cuda.Stream(dev)
     s.set_stream(stream.cuda_stream)
@@ -314,9 +317,12 @@ def run_mine(args):
     mean_solve_ms = float(np.mean(solve_ms))
     achieved = upd * b_vu / (mean_solve_ms * 1e-3) / 1e9
     out = {
-        "metric": METRICS[args.workload], "value": world * args.steps / (max_ms * 1e-3), "unit": UNIT, "n_gpus": world,
+        "metric": (METRICS[args.workload] if args.precision == "fp64" else
+                   METRICS[args.workload].replace("bit-exact vs FP64 oracle", "FP32 local solves, error vs FP64 oracle")),
+        "value": world * args.steps / (max_ms * 1e-3), "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": max_ms / args.steps,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if args.precision == "fp64" else "f32 local solves, f64 where inconclusive",
         "data": "synthetic (seeded slab mesh, conduction field and stimuli)", "config": cfg,
         "solve_ms": mean_solve_ms, "metric_ms": float(np.mean(metric_ms)),
         "iterations": stats["iterations"], "vertex_updates": upd,
@@ -340,12 +346,15 @@ def run_mine(args):
                      "gain_vs_default": (tune["default_ms"] / tune["tuned_ms"]) if tune["tuned_ms"] else None,
                      "candidates": tune["candidates"]},
     }
-    if world == 1 and not args.no_cpu_baseline:
+    if world == 1 and (not args.no_cpu_baseline or args.precision == "fp32"):
         phi_o, _, ost = oracle_solve(case)
         cores = os.cpu_count()
         out["cpu_baseline"] = {"value": 1.0 / ost["solve_s"], "unit": UNIT, "cores": cores, "kind": "port",
                                "sample": "one full solve of the same slab (metric + FIM) by the FP64 C oracle"}
-        out["parity"] = parity_report(phi_dev, phi_o)
+        out["parity"] = parity_report(phi_dev, phi_o, "max |dt| <= 1e-4 max(t)" if args.precision == "fp32" else
+                                      "max |dt| <= 1e-4 max(t); achieved bit-exact")
+        if args.precision == "fp32":
+            out["parity"]["within_tolerance"] = out["parity"]["max_rel_err"] <= 1e-4
     s.close()
     print(json.dumps(out), flush=True)
 

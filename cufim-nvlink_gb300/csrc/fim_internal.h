@@ -111,6 +111,7 @@ struct FimParams {
   int32_t two_phase;       // 1: two grid-synchronised phases per iteration (endless window only)
   int32_t dag_warps;       // warps running the FP64 tet prefix groups of a batch (1..kDagWarpsMax)
   int32_t resume;          // 1: keep the times and states as they are (no reset, no seeding)
+  int32_t fp32;            // 1: FP32 local solves where their screens are conclusive (not bit-exact)
 };
 
 // Most warps of a batch that run FP64 tet prefix groups (the scratch is

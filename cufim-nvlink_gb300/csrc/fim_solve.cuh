@@ -386,7 +386,7 @@ struct ListOut {
 // all corners (cuda_fim.h:1362-1411).
 template <int MODE>
 __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, int32_t n, double lower,
-                             float lower_lo, float lower_hi, double phi_start, double dt, bool exact_all,
+                             float lower_lo, float lower_hi, double phi_start, double dt, bool exact_all, bool fp32,
                              uint32_t stamp, int dag_warps, const ListOut &lo_, int64_t &n_filtered,
                              int64_t &n_exact)
 {
@@ -632,7 +632,11 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
 #pragma unroll
           for (int i = 0; i < 3; ++i) {
             const float le = in ? re_lo(re_in(sh.pf[j][i]) + re_len(sh.sf[j][i])) : 0.f;
-            const bool need = in && ((m >> i) & 1u) && !(le > bhi);
+            bool need = in && ((m >> i) & 1u) && !(le > bhi);
+            if (fp32 && need) {  // FP32 mode: the float edge sum is the value
+              atomicMin(&sh.res[slot], dkey((double)(sh.pf[j][i] + sh.sf[j][i])));
+              need = false;
+            }
             queue_exact(d, ph, sh, need, 2, i, slot, j, le, lane);
           }
           continue;
@@ -652,6 +656,10 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
             if (!exact_all && cb.some && cb.ub < INFINITY) atomicMin(&sh.bhi[slot], fkey(cb.ub));
             lb = isnan(cb.lb) ? -INFINITY : cb.lb;
             need = cb.some && !(lb > funkey(sh.bhi[slot]));
+            if (fp32 && need && cb.ub < INFINITY && !isnan(cb.lb)) {  // FP32 mode: conclusive screen
+              atomicMin(&sh.res[slot], dkey((double)(0.5f * (cb.lb + cb.ub))));
+              need = false;
+            }
           }
           queue_exact(d, ph, sh, need, 0, 3, slot, j, lb, lane);
         } else {
@@ -690,6 +698,10 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
               if (!exact_all && cb[h].some && cb[h].ub < INFINITY) atomicMin(&sh.bhi[sl[h]], fkey(cb[h].ub));
               lb = isnan(cb[h].lb) ? -INFINITY : cb[h].lb;
               need = cb[h].some && !(lb > funkey(sh.bhi[sl[h]]));
+              if (fp32 && need && cb[h].ub < INFINITY && !isnan(cb[h].lb)) {  // FP32 mode: conclusive screen
+                atomicMin(&sh.res[sl[h]], dkey((double)(0.5f * (cb[h].lb + cb[h].ub))));
+                need = false;
+              }
             }
             queue_exact(d, ph, sh, need, 1, kk[h], sl[h], jj[h], lb, lane);
           }
@@ -972,7 +984,7 @@ __global__ void __launch_bounds__(kThreads, 1) fim_solve_kernel(FimDev d, FimPar
       if (TWO) {
         // X -- update the narrow list, mark the downwind neighbours of the
         // vertices frozen now (cuda_fim.cu:2102-2205)
-        update_phase<kNarrow2>(d, sh, lst, nn, lower, lower_lo, lower_hi, phi_start, p.dt, p.exact_all != 0, stamp, dag,
+        update_phase<kNarrow2>(d, sh, lst, nn, lower, lower_lo, lower_hi, phi_start, p.dt, p.exact_all != 0, p.fp32 != 0, stamp, dag,
                                lo, my_evals, my_exact);
         my_updates += (gtid == 0) ? nn : 0;
         if (!grid_sync_probed(d, nblocks, p.timeout_ns, ++where)) return;
@@ -1010,7 +1022,7 @@ __global__ void __launch_bounds__(kThreads, 1) fim_solve_kernel(FimDev d, FimPar
         }
         PROBE(kPrLight);
         const int32_t nm = ld_volatile_i32(&ctl->n_marked[s]);
-        update_phase<kMarked2>(d, sh, d.lmarked, nm, lower, lower_lo, lower_hi, phi_start, p.dt, p.exact_all != 0,
+        update_phase<kMarked2>(d, sh, d.lmarked, nm, lower, lower_lo, lower_hi, phi_start, p.dt, p.exact_all != 0, p.fp32 != 0,
                                stamp, dag, lo, my_evals, my_exact);
         my_updates += (gtid == 0) ? nm : 0;
         ++it;
@@ -1018,7 +1030,7 @@ __global__ void __launch_bounds__(kThreads, 1) fim_solve_kernel(FimDev d, FimPar
         if (!grid_sync_probed(d, nblocks, p.timeout_ns, ++where)) return;
       } else {
         // P1 -- solve on elements + reduce per vertex (cuda_fim.cu:2102-2163)
-        update_phase<kNarrow4>(d, sh, lst, nn, lower, lower_lo, lower_hi, phi_start, p.dt, p.exact_all != 0, stamp, dag,
+        update_phase<kNarrow4>(d, sh, lst, nn, lower, lower_lo, lower_hi, phi_start, p.dt, p.exact_all != 0, p.fp32 != 0, stamp, dag,
                                lo, my_evals, my_exact);
         my_updates += (gtid == 0) ? nn : 0;
         if (!grid_sync_probed(d, nblocks, p.timeout_ns, ++where)) return;
@@ -1054,7 +1066,7 @@ __global__ void __launch_bounds__(kThreads, 1) fim_solve_kernel(FimDev d, FimPar
 
         // P3 -- solve elements for neighbours + reduce (cuda_fim.cu:2215-2289)
         const int32_t nm = ld_volatile_i32(&ctl->n_marked[s]);
-        update_phase<kMarked4>(d, sh, d.lmarked, nm, lower, lower_lo, lower_hi, phi_start, p.dt, p.exact_all != 0,
+        update_phase<kMarked4>(d, sh, d.lmarked, nm, lower, lower_lo, lower_hi, phi_start, p.dt, p.exact_all != 0, p.fp32 != 0,
                                stamp, dag, lo, my_evals, my_exact);
         my_updates += (gtid == 0) ? nm : 0;
         if (!grid_sync_probed(d, nblocks, p.timeout_ns, ++where)) return;

@@ -697,6 +697,7 @@ static void solve_args(const fim_solver *s, FimDev &d, FimParams &p)
   p.max_iter = s->opts.max_iterations > 0 ? s->opts.max_iterations : 10000000;
   p.timeout_ns = (uint64_t)(s->opts.timeout_s * 1e9);
   p.exact_all = s->opts.exact_all ? 1 : 0;
+  p.fp32 = (s->opts.fp32_update && !s->opts.exact_all) ? 1 : 0;
   p.two_phase = two_phase_ok(p) ? 1 : 0;
 }
 
@@ -1075,6 +1076,7 @@ extern "C" int fim_solve_noalloc(fim_solver *s, int64_t n, const int64_t *vertic
   p.timeout_ns = (uint64_t)(s->opts.timeout_s * 1e9);
   p.withhold_block = 0;
   p.exact_all = s->opts.exact_all ? 1 : 0;
+  p.fp32 = (s->opts.fp32_update && !s->opts.exact_all) ? 1 : 0;
   p.two_phase = two_phase_ok(p) ? 1 : 0;
   p.dag_warps = s->dag_warps;
   CUDA_TRY(s, cudaMemsetAsync(sc.ctl, 0, sizeof(FimCtl), st));

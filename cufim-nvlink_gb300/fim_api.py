@@ -39,7 +39,7 @@ class FimOpts(C.Structure):
     _fields_ = [("device", C.c_int), ("dt", C.c_double), ("n_steps", C.c_int), ("front_width", C.c_double),
                 ("apd", C.c_double), ("max_iterations", C.c_int64), ("timeout_s", C.c_double),
                 ("verbose", C.c_int), ("test_withhold_block", C.c_int), ("exact_all", C.c_int),
-                ("autotune", C.c_int)]
+                ("autotune", C.c_int), ("fp32_update", C.c_int)]
 
 
 class FimStats(C.Structure):

@@ -76,6 +76,12 @@ typedef struct {
                               results are identical, only slower (cross-check)     */
   int autotune;          /* 1: the first fim_solve after fim_set_mesh (or
                               fim_batch_solve after an add) runs fim_autotune first */
+  int fp32_update;       /* 1: take each triangle, tet and edge candidate's FP32
+                              value wherever its running-error screen is
+                              conclusive, FP64 only where it is not (the
+                              degenerate branch).  NOT bit-exact: the
+                              reference's freeze rule amplifies float rounding;
+                              bench.py --precision fp32 reports the error   */
 } fim_opts;
 
 /* Defaults: device 0, one endless window, reference front width, APD off. */
