@@ -43,6 +43,13 @@ class CudaSolverFIM {
   template <class EkData>
   explicit CudaSolverFIM(const EkData &ek)
   {
+    init(stage(ek));
+  }
+
+  // What the constructor stages from ek_data, without touching the GPU.
+  template <class EkData>
+  static fim_run_input stage(const EkData &ek)
+  {
     fim_run_input in;
     const auto &mesh = ek.mesh;
     in.xyz.assign(mesh.xyz.begin(), mesh.xyz.end());
@@ -68,7 +75,7 @@ class CudaSolverFIM {
     }
     in.dt = ek.opts.dt;
     in.n_steps = (int64_t)ek.opts.n_steps;
-    init(in);
+    return in;
   }
   ~CudaSolverFIM();
   CudaSolverFIM(const CudaSolverFIM &) = delete;
