@@ -52,7 +52,10 @@ METRICS = {
     "shell": "shell solves/s (4.2M-vertex ventricle-like shell FIM, bit-exact vs FP64 oracle)",
     "batch": "batched solves/s (uneven Kuhn boxes, one persistent launch, bit-exact vs FP64 oracle)",
     "warm": "warm-started vs cold FIM solves/s (learned per-vertex start times, slab family)",
+    "part": "partitioned slab solves/s (1.03M vertices, 2,964 submeshes, 50 windows, bit-exact vs FP64 oracle)",
 }
+PART_BLOCKS = (38, 13, 6)   # the slab's geometric partition: ~2,000 tets per submesh
+PART_DT, PART_STEPS = 2.0, 50
 UNIT = "solves/s"
 
 
@@ -62,10 +65,11 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["mine", "reference"], default="mine")
-    ap.add_argument("--workload", choices=["slab", "cube", "shell", "batch", "warm"], default="slab",
+    ap.add_argument("--workload", choices=["slab", "cube", "shell", "batch", "warm", "part"], default="slab",
                     help="slab: 1M-vertex anisotropic slab (default); cube: 9,261-vertex unit cube, isotropic; "
                          "shell: 4.2M-vertex ventricle-like shell; batch: many uneven solves in one launch; "
-                         "warm: learned warm start against the cold start")
+                         "warm: learned warm start against the cold start; part: the slab partitioned into "
+                         "submeshes, solved in time windows (the reference's own operating mode)")
     ap.add_argument("--batch", type=str, default="32,256,10000,500000",
                     help="batch workload: meshes,solves,min vertices,max vertices")
     ap.add_argument("--cells", type=str, default=None, help="override slab cells, e.g. 66,23,10")
@@ -99,6 +103,19 @@ def workload(args):
     cells = tuple(int(x) for x in args.cells.split(",")) if args.cells else SLAB_CELLS
     case = fim_mesh.slab_case(cells=cells)
     nV, nT = case["xyz"].shape[0], case["tets"].shape[0]
+    if args.workload == "part":
+        blocks = tuple(max(1, round(b * c / s)) for b, c, s in zip(PART_BLOCKS, cells, SLAB_CELLS))
+        case["tags"] = fim_mesh.block_tags(case["xyz"], case["tets"], blocks)
+        nparts = int(len(np.unique(case["tags"])))
+        case["dt"], case["n_steps"] = PART_DT, PART_STEPS
+        return case, {"workload": (f"anisotropic slab {cells[0]}x{cells[1]}x{cells[2]} Kuhn cells ({nV} vertices, "
+                                   f"{nT} tets) as in the slab workload, partitioned geometrically into {nparts} "
+                                   f"submeshes ({blocks[0]}x{blocks[1]}x{blocks[2]} blocks, ~{nT // nparts} tets "
+                                   f"each), {PART_STEPS} windows of {PART_DT} ms with the interface sync between "
+                                   "them (the reference's compute_step / sync_step2 semantics; APD 3e5, which "
+                                   "never fires at these times)"),
+                      "vertices": nV, "tets": nT, "submeshes": nparts, "windows": PART_STEPS, "dt_ms": PART_DT,
+                      "seed": 2, "l2": "inputs larger than L2", "parallelism": "replicas"}
     cfg = {
         "workload": (f"anisotropic slab 20x7x3 mm, {cells[0]}x{cells[1]}x{cells[2]} Kuhn cells "
                      f"({nV} vertices, {nT} tets), +-0.2h jitter, fibres -60..+60 deg over z, cf 0.6 / "
@@ -203,6 +220,16 @@ def oracle_solve(case, threads=0):
     obuild.build_oracle()
     from oracle import oracle as O
     nV = case["xyz"].shape[0]
+    if "tags" in case:  # submeshes and windows: the reference-semantics restatement
+        t0 = time.perf_counter()
+        slots, _, _, _ = O.reference_slots(nV, case["tets"], case["tags"])
+        geo = O.metric_geo(slots, case["xyz"], case["fib"], case["cf"], case["ct"])
+        fw = O.front_width(case["tets"].astype(np.int32), case["xyz"])
+        t1 = time.perf_counter()
+        phi, st, it = O.solve_reference(nV, case["tets"], case["tags"], geo, case["seed_v"], case["seed_t"],
+                                        case["dt"], case["n_steps"], fw, apd_us=3e5)
+        return phi, st, {"solve_s": time.perf_counter() - t1, "prep_s": t1 - t0, "iterations": it,
+                         "vertex_updates": None}
     t0 = time.perf_counter()
     slots, _, _, _ = O.reference_slots(nV, case["tets"], None)
     t1 = time.perf_counter()
@@ -238,8 +265,9 @@ def run_mine(args):
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
 
-    s = fim_api.Solver(device=local, fp32_update=1 if args.precision == "fp32" else 0)
-    s.set_mesh(case["xyz"], case["tets"])
+    s = fim_api.Solver(device=local, fp32_update=1 if args.precision == "fp32" else 0,
+                       **({"dt": case["dt"], "n_steps": case["n_steps"], "apd": 3e5} if "tags" in case else {}))
+    s.set_mesh(case["xyz"], case["tets"], case.get("tags"))
     stream = torch.cuda.Stream(dev)
     s.set_stream(stream.cuda_stream)
     fib = torch.tensor(case["fib"], dtype=torch.float64, device=dev).contiguous()

@@ -49,6 +49,8 @@ struct FimCtl {
   int32_t n_bad;                 // support check: reached times below every candidate bound
   int32_t pad2;
   unsigned long long tmin_key;   // dkey of the smallest such time
+  unsigned long long win_iter_max;  // submesh sweeps: most iterations of a block in this window
+  unsigned long long iters_total;   // submesh sweeps: iterations of all windows
 };
 
 // Everything the persistent kernel touches, as device pointers.
@@ -93,6 +95,7 @@ struct FimDev {
   const double *phi_init;     // warm start per vertex (nullptr: cold start)
   FimCtl *ctl;
   unsigned long long *probe;  // per-block phase times (builds with FIM_PROBE only), else nullptr
+  const int32_t *blk_ptr;     // [grid+1] submesh sweeps: the vertex copies each block owns (whole submeshes)
 };
 
 // Iteration stamps live in the upper 24 bits of the state word.
@@ -112,6 +115,7 @@ struct FimParams {
   int32_t dag_warps;       // warps running the FP64 tet prefix groups of a batch (1..kDagWarpsMax)
   int32_t resume;          // 1: keep the times and states as they are (no reset, no seeding)
   int32_t fp32;            // 1: FP32 local solves where their screens are conclusive (not bit-exact)
+  int32_t local;           // 1: submesh sweeps (blocks own whole submeshes within a window; four phases)
 };
 
 // Most warps of a batch that run FP64 tet prefix groups (the scratch is

@@ -344,8 +344,12 @@ __device__ __forceinline__ void set_phi_both(const FimDev &d, int64_t v, double 
 struct ListOut {
   int32_t *next;      // next iteration's narrow list
   int32_t *n_next;    // its length
-  int32_t *n_frozen;  // kNarrow4: vertices frozen now (lfrozen)
-  int32_t *n_marked;  // kNarrow2: neighbours marked now (lmarked)
+  int32_t *frozen;    // kNarrow4: vertices frozen now
+  int32_t *n_frozen;
+  int32_t *marked;    // kNarrow2: neighbours marked now
+  int32_t *n_marked;
+  uint8_t *dec;       // kMarked4: decided state per position of the marked list
+  bool local;         // the list is this block's own (submesh sweeps): no split over the grid
 };
 
 // One update phase over a vertex list.  Every block takes a contiguous part
@@ -395,8 +399,8 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
   const float *phf = MODE == kMarked2 ? d.phi2_f : d.phi_f;
   constexpr int kPer = 3;  // corners per thread and group in phase A
   const int tid = threadIdx.x, lane = tid & 31;
-  const int64_t per_block = ((int64_t)n + gridDim.x - 1) / gridDim.x;
-  const int64_t lbeg = min((int64_t)n, (int64_t)blockIdx.x * per_block);
+  const int64_t per_block = lo_.local ? (int64_t)n : ((int64_t)n + gridDim.x - 1) / gridDim.x;
+  const int64_t lbeg = lo_.local ? 0 : min((int64_t)n, (int64_t)blockIdx.x * per_block);
   const int64_t lend = min((int64_t)n, lbeg + per_block);
   int64_t pos = lbeg;
   while (pos < lend) {
@@ -797,10 +801,10 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
             d.sw[v] = ST_NEXT;
           } else if (fabs(old - nw) < (1e-6 * (1 + (old + nw) * .5))) {
             d.tst[v] = ST_FROZEN;
-            d.lfrozen[atomicAdd(lo_.n_frozen, 1)] = v;
+            lo_.frozen[atomicAdd(lo_.n_frozen, 1)] = v;
           }
         } else {
-          d.dec[pos + slot] = (nw < old) ? (uint8_t)ST_NARROW : __ldcg(d.tst + v);
+          lo_.dec[pos + slot] = (nw < old) ? (uint8_t)ST_NARROW : __ldcg(d.tst + v);
         }
       }
     } else if (MODE == kNarrow2) {
@@ -836,7 +840,7 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
           if (sw_state(w) != ST_NARROW && sw_stamp(w) != stamp && pn < pv) {
             if (atomicCAS(d.sw + v, w, sw_make(sw_state(w), stamp)) == w) {
               d.tst[v] = (uint8_t)sw_state(w);
-              d.lmarked[atomicAdd(lo_.n_marked, 1)] = v;
+              lo_.marked[atomicAdd(lo_.n_marked, 1)] = v;
             }
           }
         }
@@ -869,6 +873,123 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
   }
 }
 
+// One window of submesh sweeps: the block owns the vertex copies [c0, c1)
+// -- whole submeshes -- and runs the reference's compute_step
+// (cuda_fim.cu:1992-2334) on them until they converge, with block barriers
+// only: within a window the submeshes do not exchange times (sync_step2
+// runs only between windows), so each block iterates at its own pace.  The
+// four phases per iteration are those of the grid path (P1 update narrow,
+// P2 apply + mark, P3 re-solve, P4 apply + next list) on the block's own
+// lists (its segment of each list array) with counters in shared memory.
+// Returns false after recording an error.
+__device__ bool local_window(const FimDev &d, BatchSh &sh, const FimParams &p, double lower, float lower_lo,
+                             float lower_hi, double phi_start, double cur_time, int64_t &it, int dag,
+                             int64_t &my_evals, int64_t &my_exact, int64_t &my_updates, int where)
+{
+  __shared__ int32_t b_narrow[3], b_frozen, b_marked;
+  const int tid = threadIdx.x;
+  const int32_t c0 = d.blk_ptr[blockIdx.x], c1 = d.blk_ptr[blockIdx.x + 1];
+  int s = (int)(it % 3);
+  if (tid == 0) { b_narrow[0] = 0; b_narrow[1] = 0; b_narrow[2] = 0; b_frozen = 0; b_marked = 0; }
+  __syncthreads();
+  // update_states (cuda_fim.cu:1790-1845) on the block's copies
+  for (int32_t v = c0 + tid; v < c1; v += kThreads) {
+    uint8_t stv = (uint8_t)sw_state(d.sw[v]);
+    if (stv == ST_NEXT) { stv = ST_NARROW; d.sw[v] = stv; }
+    else if (p.apd >= 0.0 && stv == ST_FROZEN) {
+      if (!(d.phi[v] + p.apd > cur_time)) d.sw[v] = ST_TAIL;
+    } else if (p.apd >= 0.0 && stv == ST_TAIL) {
+      if (!(d.phi[v] + p.apd / 0.91 > cur_time)) {
+        set_phi_both(d, v, FIM_INF); d.sw[v] = ST_FAR;
+      }
+    }
+    if (stv == ST_NARROW) d.list[s][c0 + atomicAdd(&b_narrow[s], 1)] = v;
+  }
+  __syncthreads();
+  int64_t it_window = 0;
+  for (;;) {
+    s = (int)(it % 3);
+    const int s1 = (int)((it + 1) % 3), s2 = (int)((it + 2) % 3);
+    const int32_t nn = b_narrow[s];
+    if (nn == 0) break;
+    if ((p.max_iter > 0 && it_window >= p.max_iter) || it >= kMaxStampIterations) {
+      if (tid == 0 && atomicCAS(&d.ctl->error, KERR_NONE, KERR_MAX_ITER) == KERR_NONE) d.ctl->error_where = where;
+      return false;
+    }
+    const uint32_t stamp = (uint32_t)(it + 1);
+    const int32_t *lst = d.list[s] + c0;
+    int32_t *lnext = d.list[s1] + c0;
+    __syncthreads();  // every thread has read the counters of the last iteration
+    if (tid == 0) { b_narrow[s2] = 0; b_frozen = 0; b_marked = 0; }
+    __syncthreads();
+    ListOut lo;
+    lo.next = lnext; lo.n_next = &b_narrow[s1];
+    lo.frozen = d.lfrozen + c0; lo.n_frozen = &b_frozen;
+    lo.marked = d.lmarked + c0; lo.n_marked = &b_marked;
+    lo.dec = d.dec + c0; lo.local = true;
+
+    // P1 -- update the narrow list
+    update_phase<kNarrow4>(d, sh, lst, nn, lower, lower_lo, lower_hi, phi_start, p.dt, p.exact_all != 0,
+                           p.fp32 != 0, stamp, dag, lo, my_evals, my_exact);
+    if (tid == 0) my_updates += nn;
+    // P2 -- apply; mark the downwind neighbours of the vertices frozen now
+    for (int32_t i = tid; i < nn; i += kThreads) {
+      const int32_t v = lst[i];
+      set_phi(d, v, __ldcg(d.phi2 + v));
+    }
+    const int32_t nf = b_frozen;
+    for (int32_t i = tid / kMarkLanes; i < nf; i += kThreads / kMarkLanes) {
+      const int32_t n = lo.frozen[i];
+      const double pn = __ldcg(d.phi2 + n);
+      for (int64_t k = d.nptr[n] + tid % kMarkLanes; k < d.nptr[n + 1]; k += kMarkLanes) {
+        const int32_t v = __ldg(d.nbr + k);
+        const uint32_t w = __ldcg(d.sw + v);
+        const double pv = __ldcg(d.phi2 + v);
+        if (sw_state(w) != ST_NARROW && sw_stamp(w) != stamp && pn < pv) {
+          if (atomicCAS(d.sw + v, w, sw_make(ST_NEIG, stamp)) == w) {
+            d.tst[v] = (uint8_t)sw_state(w);
+            lo.marked[atomicAdd(&b_marked, 1)] = v;
+          }
+        }
+      }
+    }
+    __syncthreads();
+    // P3 -- re-solve the marked neighbours
+    const int32_t nm = b_marked;
+    update_phase<kMarked4>(d, sh, lo.marked, nm, lower, lower_lo, lower_hi, phi_start, p.dt, p.exact_all != 0,
+                           p.fp32 != 0, stamp, dag, lo, my_evals, my_exact);
+    if (tid == 0) my_updates += nm;
+    // P4 -- apply, decided states, next narrow list
+    for (int32_t i = tid; i < nm + nn; i += kThreads) {
+      if (i < nm) {
+        const int32_t v = lo.marked[i];
+        uint8_t sv = __ldcg(lo.dec + i);
+        const uint8_t tv = __ldcg(d.tst + v);
+        set_phi(d, v, __ldcg(d.phi2 + v));
+        if (sv == ST_NARROW) {
+          if (tv == ST_FROZEN) sv = ST_FROZEN;
+          else lnext[atomicAdd(&b_narrow[s1], 1)] = v;
+        }
+        d.sw[v] = sw_make(sv, stamp);
+      } else {
+        const int32_t v = lst[i - nm];
+        const uint32_t w = __ldcg(d.sw + v);
+        const uint8_t tv = __ldcg(d.tst + v);
+        if (sw_stamp(w) == stamp) continue;
+        if (sw_state(w) == ST_NARROW) {
+          if (tv == ST_FROZEN) d.sw[v] = ST_FROZEN;
+          else lnext[atomicAdd(&b_narrow[s1], 1)] = v;
+        }
+      }
+    }
+    ++it;
+    ++it_window;
+    __syncthreads();
+  }
+  if (tid == 0) atomicMax(&d.ctl->win_iter_max, (unsigned long long)it_window);
+  return true;
+}
+
 // Grid barrier with its wait accounted in the phase probe.
 __device__ __forceinline__ bool grid_sync_probed(const FimDev &d, uint32_t nblocks, uint64_t timeout_ns, int where)
 {
@@ -879,10 +1000,13 @@ __device__ __forceinline__ bool grid_sync_probed(const FimDev &d, uint32_t nbloc
   return ok;
 }
 
-// TWO: two grid-synchronised phases per iteration (one endless window),
-// else four (windows); one instantiation each, so that each holds only the
-// update phases it runs.
-template <bool TWO>
+// PATH: kPathFour -- four grid-synchronised phases per iteration (windows);
+// kPathTwo -- two (one endless window); kPathLocal -- submesh sweeps (blocks
+// own whole submeshes within a window).  One instantiation each, so that each
+// holds only the update phases it runs (no spills at 128 registers).
+enum : int { kPathFour = 0, kPathTwo = 1, kPathLocal = 2 };
+#pragma nv_diag_suppress 128  // the grid-wide window code is unreachable in the submesh-sweep instantiation
+template <int PATH>
 __global__ void __launch_bounds__(kThreads, 1) fim_solve_kernel(FimDev d, FimParams p)
 {
   FimCtl *ctl = d.ctl;
@@ -947,6 +1071,18 @@ __global__ void __launch_bounds__(kThreads, 1) fim_solve_kernel(FimDev d, FimPar
       }
     }
     if (!grid_sync_probed(d, nblocks, p.timeout_ns, ++where)) return;
+    if (PATH == kPathLocal) {
+      // submesh sweeps: each block runs its own submeshes through the window
+      if (!local_window(d, sh, p, lower, lower_lo, lower_hi, phi_start, cur_time, it, dag, my_evals, my_exact,
+                        my_updates, where))
+        return;
+      if (!grid_sync_probed(d, nblocks, p.timeout_ns, ++where)) return;
+      if (gtid == 0) {  // the window took as many iterations as its slowest block
+        ctl->iters_total += ctl->win_iter_max;
+        ctl->win_iter_max = 0;
+      }
+      continue;
+    }
     // update_states (cuda_fim.cu:1790-1845) -> narrow list of this window
     for (int64_t v = gtid; v < d.nV; v += nthreads) {
       uint8_t stv = (uint8_t)sw_state(d.sw[v]);
@@ -977,11 +1113,13 @@ __global__ void __launch_bounds__(kThreads, 1) fim_solve_kernel(FimDev d, FimPar
       int32_t *lnext = d.list[s1];
       if (gtid == 0) { ctl->n_narrow[s2] = 0; ctl->n_frozen[s2] = 0; ctl->n_marked[s2] = 0; }
       ListOut lo;
-      lo.next = lnext; lo.n_next = &ctl->n_narrow[s1]; lo.n_frozen = &ctl->n_frozen[s];
-      lo.n_marked = &ctl->n_marked[s];
+      lo.next = lnext; lo.n_next = &ctl->n_narrow[s1];
+      lo.frozen = d.lfrozen; lo.n_frozen = &ctl->n_frozen[s];
+      lo.marked = d.lmarked; lo.n_marked = &ctl->n_marked[s];
+      lo.dec = d.dec; lo.local = false;
       PROBE_COUNT(kPrPhases);
 
-      if (TWO) {
+      if (PATH == kPathTwo) {
         // X -- update the narrow list, mark the downwind neighbours of the
         // vertices frozen now (cuda_fim.cu:2102-2205)
         update_phase<kNarrow2>(d, sh, lst, nn, lower, lower_lo, lower_hi, phi_start, p.dt, p.exact_all != 0, p.fp32 != 0, stamp, dag,
@@ -1137,10 +1275,12 @@ __global__ void __launch_bounds__(kThreads, 1) fim_solve_kernel(FimDev d, FimPar
     atomicAdd((unsigned long long *)&ctl->exact_evals, s_exact);
   }
   if (gtid == 0) {
-    ctl->iterations = it;
-    atomicAdd((unsigned long long *)&ctl->vertex_updates, (unsigned long long)my_updates);
+    ctl->iterations = p.local ? (int64_t)ctl->iters_total : it;
   }
+  if (my_updates) atomicAdd((unsigned long long *)&ctl->vertex_updates, (unsigned long long)my_updates);
 }
+
+#pragma nv_diag_default 128
 
 // Sets the kernels' shared-memory size and returns the largest co-resident
 // grid on `device` (the cooperative launch's limit).
@@ -1149,11 +1289,16 @@ inline cudaError_t prepare(int device, int block, int *max_grid)
   int sms = 0, per_sm = 0;
   cudaError_t e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
   if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(fim_solve_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(BatchSh));
+  e = cudaFuncSetAttribute(fim_solve_kernel<kPathFour>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)sizeof(BatchSh));
   if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(fim_solve_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(BatchSh));
+  e = cudaFuncSetAttribute(fim_solve_kernel<kPathTwo>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)sizeof(BatchSh));
   if (e != cudaSuccess) return e;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fim_solve_kernel<false>, block, sizeof(BatchSh));
+  e = cudaFuncSetAttribute(fim_solve_kernel<kPathLocal>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)sizeof(BatchSh));
+  if (e != cudaSuccess) return e;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fim_solve_kernel<kPathFour>, block, sizeof(BatchSh));
   if (e != cudaSuccess) return e;
   if (per_sm < 1) per_sm = 1;
   *max_grid = sms * per_sm;
@@ -1165,7 +1310,8 @@ inline cudaError_t launch(const FimDev &d, const FimParams &p, int grid, int blo
   FimDev dd = d;
   FimParams pp = p;
   void *args[] = {&dd, &pp};
-  const void *fn = p.two_phase ? (const void *)fim_solve_kernel<true> : (const void *)fim_solve_kernel<false>;
+  const void *fn = p.local ? (const void *)fim_solve_kernel<kPathLocal>
+                 : p.two_phase ? (const void *)fim_solve_kernel<kPathTwo> : (const void *)fim_solve_kernel<kPathFour>;
   return cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(block), args, sizeof(BatchSh), stream);
 }
 

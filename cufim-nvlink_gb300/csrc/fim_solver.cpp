@@ -90,12 +90,17 @@ struct fim_solver {
   // warps (defaults, or the autotuner's choice for the staged problem)
   int max_grid[kNumShapes] = {};
   int shape = 0, grid = 0, dag_warps = kDefaultDagWarps;
+  int local = 0;                    // submesh sweeps for meshes with several submeshes (tuned)
   bool tuned = false;
   fim_tune_info tune{};
 
   // mesh (nL vertex copies: nL == nV with one submesh)
   int64_t nV = 0, nT = 0, nC = 0, nL = 0;
   int32_t n_submeshes = 1;
+  std::vector<int64_t> h_sub_ptr;   // first vertex copy of every submesh (+ end)
+  std::vector<int64_t> h_cptr;      // corner offsets of the vertex copies (host copy)
+  DevBuf<int32_t> blk_ptr;          // submesh sweeps: copies owned by each block
+  int blk_grid = -1;                // grid blk_ptr was computed for
   std::vector<uint8_t> in_tet;
   std::vector<int64_t> h_gptr;
   std::vector<int32_t> h_gcopy;
@@ -282,6 +287,7 @@ struct Staging {
   std::vector<int32_t> slots, cslots;
   int64_t n_copies = 0;
   int32_t n_submeshes = 1;
+  std::vector<int64_t> sub_ptr;   // first vertex copy of every submesh (n_submeshes + 1)
   std::vector<int64_t> gptr;
   std::vector<int32_t> gcopy;
 };
@@ -332,6 +338,7 @@ void reference_slots(int64_t nV, int64_t nT, const int64_t *tets, const int32_t 
         S.cslots[4 * e + j] = nagg > 1 ? (int32_t)(base + rank[g[j]]) : (int32_t)g[j];
       }
     }
+    S.sub_ptr.push_back(base);
     base += next;
     for (int32_t v : touched) rank[v] = -1;
     touched.clear();
@@ -452,11 +459,14 @@ extern "C" int fim_set_mesh(fim_solver *s, int64_t nV, const double *xyz, int64_
   s->warm = nullptr;  // a warm start belongs to the previous mesh
   if (s->tuned) {      // so does a tuned launch configuration
     s->tuned = false;
-    s->shape = 0; s->grid = s->max_grid[0]; s->dag_warps = kDefaultDagWarps;
+    s->shape = 0; s->grid = s->max_grid[0]; s->dag_warps = kDefaultDagWarps; s->local = 0;
   }
   s->have_mesh = s->have_cond = s->have_stim = s->solved = false;
   s->nV = nV; s->nT = nT; s->nC = nC; s->nL = nL;
   s->n_submeshes = S.n_submeshes;
+  S.sub_ptr.push_back(nL);
+  s->h_sub_ptr.swap(S.sub_ptr);
+  s->blk_grid = -1;
   s->in_tet.swap(in_tet);
   s->h_gptr.swap(S.gptr);
   s->h_gcopy.swap(S.gcopy);
@@ -499,6 +509,8 @@ extern "C" int fim_set_mesh(fim_solver *s, int64_t nV, const double *xyz, int64_
   CUDA_TRY(s, cudaMemcpyAsync(s->tslots.p, slots.data(), sizeof(int32_t) * 4 * nT, cudaMemcpyHostToDevice, st));
   CUDA_TRY(s, cudaMemcpyAsync(s->cidx.p, cidx.data(), sizeof(int64_t) * nC, cudaMemcpyHostToDevice, st));
   CUDA_TRY(s, cudaMemcpyAsync(s->cptr.p, cptr.data(), sizeof(int64_t) * (nL + 1), cudaMemcpyHostToDevice, st));
+  CUDA_TRY(s, cudaStreamSynchronize(st));
+  s->h_cptr.swap(cptr);
   {
     // the ids part of the first-read records (the metric kernel fills the rest)
     std::vector<uint4> crec((size_t)kCrecWords * nC);
@@ -675,6 +687,23 @@ static void print_probe(fim_solver *s, int grid)
 static int tune_solver(fim_solver *s, cudaStream_t st);
 static int warm_check(fim_solver *s, cudaStream_t st);
 
+// Submesh sweeps: whole submeshes to blocks, contiguous in copy order, with
+// about the same number of corners each (the corners are the work).
+static void block_ranges(const fim_solver *s, int grid, std::vector<int32_t> &out)
+{
+  const std::vector<int64_t> &sp = s->h_sub_ptr;
+  const int nsub = (int)sp.size() - 1;
+  const int64_t total = s->h_cptr[s->nL];
+  out.assign(grid + 1, (int32_t)s->nL);
+  out[0] = 0;
+  int b = 1;
+  for (int a = 0; a < nsub && b < grid; ++a) {
+    // close block b-1 after submesh a once it holds its share
+    const int64_t done = s->h_cptr[sp[a + 1]];
+    while (b < grid && done * grid >= total * b) out[b++] = (int32_t)sp[a + 1];
+  }
+}
+
 // Launch parameters and device view of the solver's staged problem.
 static void solve_args(const fim_solver *s, FimDev &d, FimParams &p)
 {
@@ -703,8 +732,10 @@ static void solve_args(const fim_solver *s, FimDev &d, FimParams &p)
 
 // One solve with launch configuration (shape, grid, dag_warps); resume keeps
 // the times and states in place instead of resetting and seeding them.
-static int run_solve(fim_solver *s, cudaStream_t st, int shape, int grid, int dag_warps, bool resume = false)
+static int run_solve(fim_solver *s, cudaStream_t st, int shape, int grid, int dag_warps, bool resume = false,
+                     int local = -1)
 {
+  if (local < 0) local = s->local;
   FimDev d{};
   FimParams p{};
   solve_args(s, d, p);
@@ -712,6 +743,19 @@ static int run_solve(fim_solver *s, cudaStream_t st, int shape, int grid, int da
                          ? s->opts.test_withhold_block : 0;
   p.dag_warps = dag_warps;
   p.resume = resume ? 1 : 0;
+  if (local && s->n_submeshes > 1) {
+    p.local = 1;
+    p.two_phase = 0;
+    if (s->blk_grid != grid) {
+      std::vector<int32_t> ranges;
+      block_ranges(s, grid, ranges);
+      CUDA_TRY(s, s->blk_ptr.reserve(ranges.size()));
+      CUDA_TRY(s, cudaMemcpyAsync(s->blk_ptr.p, ranges.data(), sizeof(int32_t) * ranges.size(),
+                                  cudaMemcpyHostToDevice, st));
+      s->blk_grid = grid;
+    }
+    d.blk_ptr = s->blk_ptr.p;
+  }
 #ifdef FIM_PROBE
   CUDA_TRY(s, s->probe.reserve((size_t)grid * kProbeSlots));
   CUDA_TRY(s, cudaMemsetAsync(s->probe.p, 0, sizeof(unsigned long long) * grid * kProbeSlots, st));
@@ -735,6 +779,7 @@ static int run_solve(fim_solver *s, cudaStream_t st, int shape, int grid, int da
   s->stats.batch_slots = kShapes[shape].slots;
   s->stats.batch_corners = kShapes[shape].corners;
   s->stats.dag_warps = dag_warps;
+  s->stats.submesh_sweeps = p.local;
 #ifdef FIM_PROBE
   print_probe(s, grid);
 #endif
@@ -875,6 +920,7 @@ static int tune_solver(fim_solver *s, cudaStream_t st)
 {
   int n = 0;
   double def_ms = 0.0;
+  s->local = 0;
   int rc = time_config(s, st, 0, s->max_grid[0], kDefaultDagWarps, &def_ms);
   if (rc != FIM_OK) return rc;
   ++n;
@@ -896,12 +942,22 @@ static int tune_solver(fim_solver *s, cudaStream_t st)
   const int g = b_grid;
   for (int dag : {6, 8, 12})
     if ((rc = consider(b_shape, g, dag)) != FIM_OK) return rc;
+  int b_local = 0;
+  if (s->n_submeshes > 1) {  // submesh sweeps against grid-wide iterations
+    s->local = 1;
+    double ms = 0.0;
+    if ((rc = time_config(s, st, b_shape, b_grid, b_dag, &ms)) != FIM_OK) return rc;
+    ++n;
+    if (ms < b_ms) { b_ms = ms; b_local = 1; }
+  }
+  s->local = b_local;
   s->shape = b_shape; s->grid = b_grid; s->dag_warps = b_dag;
   s->tuned = true;
   s->tune.batch_slots = kShapes[b_shape].slots;
   s->tune.batch_corners = kShapes[b_shape].corners;
   s->tune.grid_blocks = b_grid;
   s->tune.dag_warps = b_dag;
+  s->tune.submesh_sweeps = b_local;
   s->tune.default_ms = def_ms;
   s->tune.tuned_ms = b_ms;
   s->tune.candidates = n;
@@ -925,7 +981,7 @@ extern "C" int fim_set_tune(fim_solver *s, const fim_tune_info *cfg)
   if (!s) return set_err(nullptr, FIM_ERR_INVALID_ARGUMENT, "fim_set_tune: solver is NULL");
   if (!cfg) {  // back to the default configuration
     s->tuned = false;
-    s->shape = 0; s->grid = s->max_grid[0]; s->dag_warps = kDefaultDagWarps;
+    s->shape = 0; s->grid = s->max_grid[0]; s->dag_warps = kDefaultDagWarps; s->local = 0;
     return FIM_OK;
   }
   int shape = -1;
@@ -944,6 +1000,7 @@ extern "C" int fim_set_tune(fim_solver *s, const fim_tune_info *cfg)
     return set_err(s, FIM_ERR_INVALID_ARGUMENT, "fim_set_tune: dag_warps %d outside [1,%d]", cfg->dag_warps,
                    kDagWarpsMax);
   s->shape = shape; s->grid = cfg->grid_blocks; s->dag_warps = cfg->dag_warps;
+  s->local = cfg->submesh_sweeps ? 1 : 0;
   s->tuned = true;
   s->tune = *cfg;
   return FIM_OK;
@@ -960,6 +1017,7 @@ extern "C" int fim_get_tune(const fim_solver *s, fim_tune_info *info)
     info->batch_corners = kShapes[s->shape].corners;
     info->grid_blocks = s->grid;
     info->dag_warps = s->dag_warps;
+    info->submesh_sweeps = s->local;
   }
   return FIM_OK;
 }

@@ -47,13 +47,13 @@ class FimStats(C.Structure):
                 ("exact_evals", C.c_int64), ("solve_ms", C.c_double), ("metric_ms", C.c_double), ("n_corners", C.c_int64),
                 ("grid_blocks", C.c_int), ("block_threads", C.c_int), ("batch_slots", C.c_int),
                 ("batch_corners", C.c_int), ("dag_warps", C.c_int), ("warm_reset", C.c_int64),
-                ("warm_rounds", C.c_int)]
+                ("warm_rounds", C.c_int), ("submesh_sweeps", C.c_int)]
 
 
 class FimTuneInfo(C.Structure):
     _fields_ = [("batch_slots", C.c_int), ("batch_corners", C.c_int), ("grid_blocks", C.c_int),
-                ("dag_warps", C.c_int), ("default_ms", C.c_double), ("tuned_ms", C.c_double),
-                ("candidates", C.c_int)]
+                ("dag_warps", C.c_int), ("submesh_sweeps", C.c_int), ("default_ms", C.c_double),
+                ("tuned_ms", C.c_double), ("candidates", C.c_int)]
 
 
 class FimPlanInfo(C.Structure):
@@ -237,14 +237,15 @@ class Solver:
         _check(lib().fim_get_tune(self.h, C.byref(t)), self.h)
         return {k: getattr(t, k) for k, _ in FimTuneInfo._fields_}
 
-    def set_tune(self, slots=None, corners=None, grid=None, dag_warps=None):
+    def set_tune(self, slots=None, corners=None, grid=None, dag_warps=None, submesh_sweeps=None):
         """Pins a launch configuration (all None: back to the default)."""
-        if slots is None and corners is None and grid is None and dag_warps is None:
+        if slots is None and corners is None and grid is None and dag_warps is None and submesh_sweeps is None:
             _check(lib().fim_set_tune(self.h, None), self.h)
             return
         cur = self.tune_info()
         t = FimTuneInfo(batch_slots=slots or cur["batch_slots"], batch_corners=corners or cur["batch_corners"],
-                        grid_blocks=grid or cur["grid_blocks"], dag_warps=dag_warps or cur["dag_warps"])
+                        grid_blocks=grid or cur["grid_blocks"], dag_warps=dag_warps or cur["dag_warps"],
+                        submesh_sweeps=cur["submesh_sweeps"] if submesh_sweeps is None else int(submesh_sweeps))
         _check(lib().fim_set_tune(self.h, C.byref(t)), self.h)
 
     def features(self, d_features):

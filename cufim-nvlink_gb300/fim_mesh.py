@@ -218,3 +218,17 @@ def shell_case(n_wall=20, n_circ=630, n_long=320, inner=(20.0, 50.0), outer=(30.
     t0 = rng.uniform(0.0, t0_max, size=n_stim)
     return dict(xyz=xyz, tets=tets, fib=fib, cf=np.full(nT, cf), ct=np.full(nT, ct), seed_v=seeds, seed_t=t0,
                 name=f"shell{n_wall}x{n_circ}x{n_long}")
+
+
+def block_tags(xyz, tets, parts):
+    """Geometric partition (this library's own, standing in for the
+    reference's METIS-style .tags input): the bounding box is cut into
+    parts[0] x parts[1] x parts[2] blocks and every tet takes the block of
+    its centroid.  Returns int32 tags numbered x-fastest."""
+    cen = tet_centroids(xyz, tets)
+    lo, hi = xyz.min(axis=0), xyz.max(axis=0)
+    idx = []
+    for a in range(3):
+        k = np.floor((cen[:, a] - lo[a]) / max(hi[a] - lo[a], 1e-300) * parts[a]).astype(np.int64)
+        idx.append(np.clip(k, 0, parts[a] - 1))
+    return (idx[0] + parts[0] * (idx[1] + parts[1] * idx[2])).astype(np.int32)

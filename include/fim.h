@@ -152,6 +152,7 @@ typedef struct {
   int dag_warps;           /* warps running FP64 tet prefixes per batch     */
   int64_t warm_reset;      /* warm start: times the support check rejected  */
   int warm_rounds;         /* warm start: check-reset-resume rounds run     */
+  int submesh_sweeps;      /* 1: blocks ran whole submeshes per window      */
 } fim_stats;
 int fim_get_stats(const fim_solver *s, fim_stats *out);
 
@@ -170,6 +171,10 @@ typedef struct {
   int batch_corners;    /* ... and corners per batch                              */
   int grid_blocks;      /* persistent blocks                                      */
   int dag_warps;        /* warps running FP64 tet prefixes                        */
+  int submesh_sweeps;   /* meshes with several submeshes: 1 = every block runs its
+                           own whole submeshes through each window with block
+                           barriers only (grid barriers only between windows),
+                           0 = grid-wide iterations; results are identical     */
   double default_ms;    /* solve time with the default configuration (0: untuned) */
   double tuned_ms;      /* solve time with the chosen one                         */
   int candidates;       /* configurations timed                                   */
@@ -181,7 +186,7 @@ int fim_get_tune(const fim_solver *s, fim_tune_info *info);
  * batch_slots/batch_corners must name a compiled batch shape (192x4096,
  * 160x3072, 96x2048), grid_blocks lie in [1, the shape's co-resident grid],
  * dag_warps in [1, 12]; the timing fields are ignored.  NULL restores the
- * default configuration. */
+ * default configuration (grid-wide iterations). */
 int fim_set_tune(fim_solver *s, const fim_tune_info *cfg);
 
 /* Allocation-free re-solve -- no counterpart in the reference.

@@ -136,3 +136,37 @@ def test_autotune_option_and_batch(F, O):
             phi_o, st_o, _ = _oracle(O, k)
             phi, st = b.times(i)
             _same(phi, st, phi_o, st_o)
+
+
+@pytest.mark.parametrize("parts", [(3, 2, 2), (8, 3, 2)])
+def test_submesh_sweeps_equal_grid_iterations(F, O, parts):
+    """A partitioned slab with time windows: the submesh sweeps (each block
+    runs whole submeshes through a window with block barriers only) and the
+    grid-wide iterations give the oracle's reference-semantics result bit
+    for bit, in the same number of iterations."""
+    import fim_mesh
+    c = fim_mesh.slab_case(cells=(40, 14, 6), size=(20.0, 7.0, 3.0), seed=5)
+    xyz, tets = c["xyz"], c["tets"]
+    tags = fim_mesh.block_tags(xyz, tets, parts)
+    nV = xyz.shape[0]
+    dt, steps = 3.0, 30
+    slots, _, _, _ = O.reference_slots(nV, tets, tags)
+    geo = O.metric_geo(slots, xyz, c["fib"], c["cf"], c["ct"])
+    fw = O.front_width(tets.astype(np.int32), xyz)
+    phi_o, st_o, _ = O.solve_reference(nV, tets, tags, geo, c["seed_v"], c["seed_t"], dt, steps, fw)
+    iters = []
+    for local in (1, 0):
+        with F.Solver(dt=dt, n_steps=steps, apd=3e5) as s:
+            s.set_mesh(xyz, tets, tags)
+            s.set_conduction(c["fib"], c["cf"], c["ct"])
+            s.set_stimuli(c["seed_v"], c["seed_t"])
+            s.set_tune(submesh_sweeps=local)
+            s.solve()
+            st = s.stats()
+            assert st["submesh_sweeps"] == local
+            phi, sts = s.times()
+        _same(phi, sts, phi_o, st_o)
+        iters.append(st["iterations"])
+    # a window takes as many iterations as its slowest submesh either way
+    # (the oracle counts every submesh's own iterations instead)
+    assert iters[0] == iters[1]
