@@ -52,7 +52,10 @@ enum : int { kPrSetup = 0, kPrA, kPrB, kPrS, kPrD, kPrE, kPrMark, kPrBarrier, kP
 // FP64 pipe for 64 cycles whatever its active lanes, so two blocks per SM
 // would stack their FP64 warps on the same sub-partitions).
 constexpr int kThreads = kSolveThreads;  // threads per block of the solve kernel
-constexpr int kMarkLanes = 16;           // threads per frozen vertex in the neighbour marking
+#ifndef FIM_MARK_LANES
+#define FIM_MARK_LANES 16
+#endif
+constexpr int kMarkLanes = FIM_MARK_LANES;  // threads per frozen vertex in the neighbour marking
 static_assert(kThreads % kMarkLanes == 0, "marking groups must tile the grid");
 constexpr int kSlots = FIM_SLOTS;             // vertices per batch (at most)
 constexpr int kCornerCap = FIM_CORNER_CAP;    // corners per batch
@@ -397,7 +400,12 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
   constexpr bool kMarkedMode = is_marked_mode(MODE);
   const double *ph = MODE == kMarked2 ? d.phi2 : d.phi;      // times this phase reads
   const float *phf = MODE == kMarked2 ? d.phi2_f : d.phi_f;
-  constexpr int kPer = 3;  // corners per thread and group in phase A
+#ifndef FIM_APER
+#define FIM_APER 1
+#endif
+  // corners per thread and round in phase A: one (12.44 ms on the 1M slab)
+  // beats the hand-batched loads of two (12.55) and three (12.92)
+  constexpr int kPer = FIM_APER;
   const int tid = threadIdx.x, lane = tid & 31;
   const int64_t per_block = lo_.local ? (int64_t)n : ((int64_t)n + gridDim.x - 1) / gridDim.x;
   const int64_t lbeg = lo_.local ? 0 : min((int64_t)n, (int64_t)blockIdx.x * per_block);
