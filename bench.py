@@ -75,6 +75,7 @@ def parse_args():
     ap.add_argument("--cells", type=str, default=None, help="override slab cells, e.g. 66,23,10")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch configuration")
+    ap.add_argument("--no-extra", action="store_true", help="skip the short runs of the other workloads")
     ap.add_argument("--precision", choices=["fp64", "fp32"], default="fp64",
                     help="fp32: FP32 local solves wherever their screens are conclusive (not bit-exact; the "
                          "parity block reports the error against the FP64 oracle)")
@@ -384,7 +385,92 @@ def run_mine(args):
         if args.precision == "fp32":
             out["parity"]["within_tolerance"] = out["parity"]["max_rel_err"] <= 1e-4
     s.close()
+    if world == 1 and args.workload == "slab" and args.cells is None and not args.no_extra:
+        out["other_workloads"] = other_workloads(args)
     print(json.dumps(out), flush=True)
+
+
+def other_workloads(args):
+    """Short measurements of the other workload families in the same run, so
+    that they are not only reported by separate invocations: the unit cube
+    (bit-exact check against the oracle), the slab partitioned into 2,964
+    submeshes with 50 windows, and a scaled batch of 32 uneven solves in one
+    launch against the same solves one at a time.  Device time of the solves
+    (the conduction is staged once), each configuration autotuned first."""
+    import fim_api
+    import fim_mesh
+    from oracle import build as obuild
+    from oracle import oracle as O
+    obuild.build_oracle()
+    res = {}
+    reps = max(3, min(args.steps, 10))
+
+    def timed(solver, n):
+        ms = []
+        for _ in range(n):
+            solver.solve()
+            ms.append(solver.stats()["solve_ms"])
+        return float(np.median(ms))
+
+    # unit cube (the plain FIM configuration)
+    c = fim_mesh.cube_case(20)
+    nV = c["xyz"].shape[0]
+    with fim_api.Solver() as s:
+        s.set_mesh(c["xyz"], c["tets"])
+        s.set_conduction(c["fib"], c["cf"], c["ct"])
+        s.set_stimuli(c["seed_v"], c["seed_t"])
+        tune = s.autotune()
+        ms = timed(s, reps)
+        phi = s.times(with_state=False)
+    slots, _, _, _ = O.reference_slots(nV, c["tets"], None)
+    geo = O.metric_geo(slots, c["xyz"], c["fib"], c["cf"], c["ct"])
+    phi_o, _, _, _ = O.solve_pure(nV, slots, geo, c["seed_v"], c["seed_t"])
+    res["cube"] = {"workload": f"unit cube 20^3 Kuhn cells ({nV} vertices), isotropic 0.6, stimulus at the origin",
+                   "solves_per_s": 1e3 / ms, "solve_ms": ms, "n_bit_mismatch_vs_oracle": int(np.count_nonzero(phi != phi_o)),
+                   "autotune": {k: tune[k] for k in ("batch_slots", "batch_corners", "grid_blocks", "dag_warps")}}
+    # the slab in submeshes and windows (the reference's operating mode)
+    p = fim_mesh.slab_case(cells=SLAB_CELLS)
+    tags = fim_mesh.block_tags(p["xyz"], p["tets"], PART_BLOCKS)
+    with fim_api.Solver(dt=PART_DT, n_steps=PART_STEPS, apd=3e5) as s:
+        s.set_mesh(p["xyz"], p["tets"], tags)
+        s.set_conduction(p["fib"], p["cf"], p["ct"])
+        s.set_stimuli(p["seed_v"], p["seed_t"])
+        tune = s.autotune()
+        ms = timed(s, max(3, reps // 2))
+        st = s.stats()
+    res["part"] = {"workload": (f"the 1.03M-vertex slab in {int(len(np.unique(tags)))} submeshes, {PART_STEPS} windows "
+                                f"of {PART_DT} ms (bit-exact test: tests/test_gpu_tune.py; full check: bench.py "
+                                "--workload part)"),
+                   "solves_per_s": 1e3 / ms, "solve_ms": ms, "iterations": st["iterations"],
+                   "vertex_updates": st["vertex_updates"], "submesh_sweeps_chosen": tune["submesh_sweeps"]}
+    # a scaled batch: 32 solves over 8 uneven boxes in one launch
+    meshes, solves = fim_mesh.batch_cases(n_meshes=8, n_solves=32, vmin=12_000, vmax=96_000)
+    with fim_api.Batch() as b:
+        for sv in solves:
+            m = meshes[sv["mesh"]]
+            b.add(m["xyz"], m["tets"], sv["fib"], sv["cf"], sv["ct"], sv["seed_v"], sv["seed_t"])
+        b.autotune()
+        bms = []
+        for _ in range(reps):
+            b.solve()
+            bms.append(b.stats()["solve_ms"])
+        bms = float(np.median(bms))
+    seq = 0.0
+    with fim_api.Solver() as s:
+        cur = -1
+        for sv in solves:
+            m = meshes[sv["mesh"]]
+            if sv["mesh"] != cur:
+                s.set_mesh(m["xyz"], m["tets"])
+                cur = sv["mesh"]
+            s.set_conduction(sv["fib"], sv["cf"], sv["ct"])
+            s.set_stimuli(sv["seed_v"], sv["seed_t"])
+            s.solve()
+            seq += s.stats()["solve_ms"]
+    res["batch_scaled"] = {"workload": "32 solves over 8 jittered Kuhn boxes of 12k-96k vertices, one launch",
+                           "solves_per_s": 32e3 / bms, "batch_ms": bms, "sequential_solves_per_s": 32e3 / seq,
+                           "speedup_vs_sequential": seq / bms}
+    return res
 
 
 def run_reference(args):

@@ -26,7 +26,10 @@ constexpr int kCgfStride = 8;
 constexpr int kCrecWords = 2;
 
 // Threads per block of the persistent solve kernel (one block per SM).
-constexpr int kSolveThreads = 512;
+#ifndef FIM_SOLVE_THREADS
+#define FIM_SOLVE_THREADS 512
+#endif
+constexpr int kSolveThreads = FIM_SOLVE_THREADS;
 
 // Kernel error codes written into FimCtl::error.
 enum : int { KERR_NONE = 0, KERR_TIMEOUT = 1, KERR_MAX_ITER = 2 };

@@ -65,7 +65,7 @@ constexpr int kQcap = 768;          // exact solves queued per kind and batch (m
 // Phase D runs the queued tets on at most FimParams::dag_warps (<=
 // kDagWarpsMax) warps, one group of kDagLanes lanes per tet (scratch:
 // kDagGroups * kDagSlots doubles).
-constexpr int kDagWarps = kDagWarpsMax;
+constexpr int kDagWarps = kDagWarpsMax * 32 <= kThreads ? kDagWarpsMax : kThreads / 32;
 constexpr int kDagGroups = kDagWarps * 32 / kDagLanes;
 
 // Update phases.  With windows (finite dt) an iteration runs the reference's
