@@ -633,6 +633,12 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
         if (lane == 0) cl = atomicAdd(&sh.next_item, 32);
         cl = __shfl_sync(FULL_MASK, cl, 0);
         if (cl >= nclaim) break;
+#ifdef FIM_PROBE
+        const unsigned long long pt0 = global_timer();
+#define PROBE_CHUNK(k) do { if (lane == 0) atomicAdd(&d.probe[blockIdx.x * kProbeSlots + (k)], global_timer() - pt0); } while (0)
+#else
+#define PROBE_CHUNK(k) ((void)0)
+#endif
         if (cl >= edge_c0) {
           // the edges that can still be the minimum
           const int j = cl - edge_c0 + lane;
@@ -651,6 +657,7 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
             }
             queue_exact(d, ph, sh, need, 2, i, slot, j, le, lane);
           }
+          PROBE_CHUNK(13);
           continue;
         }
         const int ib = cl < tri0 ? cl : tri0 + 2 * (cl - tri0);  // 32 claimed in the triangle range stand for 64
@@ -674,6 +681,7 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
             }
           }
           queue_exact(d, ph, sh, need, 0, 3, slot, j, lb, lane);
+          PROBE_CHUNK(11);
         } else {
           int jj[2], kk[2], sl[2];
           bool in[2];
@@ -717,7 +725,9 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
             }
             queue_exact(d, ph, sh, need, 1, kk[h], sl[h], jj[h], lb, lane);
           }
+          PROBE_CHUNK(12);
         }
+#undef PROBE_CHUNK
       }
     }
     __syncthreads();

@@ -671,13 +671,13 @@ static void print_probe(fim_solver *s, int grid)
   if (cudaMemcpy(h.data(), s->probe.p, sizeof(unsigned long long) * h.size(), cudaMemcpyDeviceToHost) != cudaSuccess)
     return;
   static const char *names[kProbeSlots] = {"setup", "A", "B", "S", "D", "E", "mark", "barrier", "light", "batches",
-                                           "phases", "", "", "", "", ""};
+                                           "phases", "S-tet warp-ms", "S-tri warp-ms", "S-edge warp-ms", "", ""};
   std::fprintf(stderr, "probe (mean per block):");
-  for (int k = 0; k < 11; ++k) {
+  for (int k = 0; k < 14; ++k) {
     double sum = 0.0;
     for (int b = 0; b < grid; ++b) sum += (double)h[(size_t)b * kProbeSlots + k];
     sum /= grid;
-    if (k < 9) std::fprintf(stderr, " %s %.3f ms", names[k], sum * 1e-6);
+    if (k < 9 || k >= 11) std::fprintf(stderr, " %s %.3f ms", names[k], sum * 1e-6);
     else std::fprintf(stderr, " %s %.1f", names[k], sum);
   }
   std::fprintf(stderr, "\n");
