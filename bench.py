@@ -672,7 +672,7 @@ def run_warm(args):
                                 "random cf/ct/fibre/scar/stimuli, solved in one batched launch from the learned start; "
                                 "network 7->128->128->128->1 trained on 400 maps, 3000 Adam steps of 4096 vertices; "
                                 "start = 1.05 x prediction"), "train_maps": 400, "test_maps": n_test},
-        "north_star_ratio": {"value": warm_batched / cold_single,
+        "warm_batched_over_cold_single": {"value": warm_batched / cold_single,
                              "how": "warm-started batched solves/s / plain cold-start single-solve GPU FIM solves/s",
                              "cold_batched_over_cold_single": cold_batched / cold_single,
                              "warm_batched_over_cold_batched": warm_batched / cold_batched},
