@@ -124,7 +124,7 @@ struct BatchSh {
   union {
     struct {
       float pf[kCornerCap][3];      // their float times
-      float sf[kCornerCap][3];      // float edge lengths sqrt(e14), sqrt(e24), sqrt(e34)
+      float sf[kCornerCap][3];      // float edge lengths sqrt(e14), sqrt(e24), sqrt(e34); in the exact mode phase A replaces them by the edges' lower bounds
     };
     double dag[kDagGroups][kDagSlots];  // phase D (where pf and sf are dead): scratch of the tet prefix groups
   };
@@ -134,9 +134,10 @@ struct BatchSh {
   // compacted screen lists: items corner j | pair k << 14 (triangles), corner j (tets)
   uint16_t tri[kTriCap];
   uint16_t tet[kTetCap];
+  uint16_t edg[kCornerCap];         // corners whose best edge can still be the minimum (phase B): never full
   uint32_t q[3][kQcap];             // queued exact solves: [0] tets, [1] triangles, [2] edges
   float qlb[3][kQcap];              // their lower bounds (rechecked against the final bhi)
-  int ntri, ntet, nq[3];
+  int ntri, ntet, nedge, nq[3];
   int next_item;                    // next unclaimed screen item (phase S)
   int nslot;                        // vertices of the current batch
   int nfz;                          // kNarrow2: frozen slots of the batch
@@ -433,7 +434,7 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
     }
     if (tid == 0) {
       sh.cp[0] = 0;
-      sh.ntri = 0; sh.ntet = 0; sh.nq[0] = 0; sh.nq[1] = 0; sh.nq[2] = 0; sh.next_item = 0; sh.nfz = 0;
+      sh.ntri = 0; sh.ntet = 0; sh.nedge = 0; sh.nq[0] = 0; sh.nq[1] = 0; sh.nq[2] = 0; sh.next_item = 0; sh.nfz = 0;
     }
     __syncthreads();
     if (tid < 32) {
@@ -536,7 +537,11 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
           }
           if (ok) {
             m |= 1u << i;
-            ub = fminf(ub, re_hi(P + re_len(sh.sf[j][i])));
+            const Re E = P + re_len(sh.sf[j][i]);
+            ub = fminf(ub, re_hi(E));
+            if (!fp32) sh.sf[j][i] = re_lo(E);  // exact mode: the edge's lower bound replaces its length
+          } else if (!fp32) {
+            sh.sf[j][i] = INFINITY;
           }
           sh.pf[j][i] = pf[r][i];
         }
@@ -609,6 +614,15 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
         const int p = warp_append(&sh.ntet, need, lane);
         if (p >= 0) sh.tet[p] = (uint16_t)j;  // kTetCap == kCornerCap: never full
       }
+      {
+        // the corners with an edge that can still be the minimum: the
+        // smallest edge lower bound (phase A) against bhi; the FP32 mode
+        // lists every corner with a valid edge
+        bool need = false;
+        if (in) need = fp32 ? m != 0u : !(fminf(sh.sf[j][0], fminf(sh.sf[j][1], sh.sf[j][2])) > bhi);
+        const int p = warp_append(&sh.nedge, need, lane);
+        if (p >= 0) sh.edg[p] = (uint16_t)j;  // one entry per corner at most: never full
+      }
     }
     __syncthreads();
     PROBE(kPrB);
@@ -625,7 +639,8 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
       const int ntet = min(sh.ntet, kTetCap), ntri = min(sh.ntri, kTriCap);
       const int tri0 = (ntet + 31) & ~31;
       const int edge_c0 = tri0 + ((ntri + 63) / 64) * 32;  // claim index of the first edge chunk
-      const int nclaim = edge_c0 + ((kept + 31) & ~31);
+      const int nedge = sh.nedge;
+      const int nclaim = edge_c0 + ((nedge + 31) & ~31);
       for (;;) {
         // claims of 32: tet chunks, then triangle chunks of 64 (two per
         // lane), then edge chunks of 32 corners
@@ -640,16 +655,19 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
 #define PROBE_CHUNK(k) ((void)0)
 #endif
         if (cl >= edge_c0) {
-          // the edges that can still be the minimum
-          const int j = cl - edge_c0 + lane;
-          const bool in = j < kept;
+          // the edges that can still be the minimum, over the corners phase
+          // B listed (sf holds the edges' lower bounds, or their lengths in
+          // the FP32 mode)
+          const int e = cl - edge_c0 + lane;
+          const bool in = e < nedge;
+          const int j = in ? (int)sh.edg[e] : 0;
           int slot = 0;
           uint32_t m = 0;
           float bhi = 0.f;
           if (in) { slot = sh.cs[j]; m = sh.vm[j]; bhi = funkey(sh.bhi[slot]); }
 #pragma unroll
           for (int i = 0; i < 3; ++i) {
-            const float le = in ? re_lo(re_in(sh.pf[j][i]) + re_len(sh.sf[j][i])) : 0.f;
+            const float le = !in ? 0.f : (fp32 ? re_lo(re_in(sh.pf[j][i]) + re_len(sh.sf[j][i])) : sh.sf[j][i]);
             bool need = in && ((m >> i) & 1u) && !(le > bhi);
             if (fp32 && need) {  // FP32 mode: the float edge sum is the value
               atomicMin(&sh.res[slot], dkey((double)(sh.pf[j][i] + sh.sf[j][i])));
