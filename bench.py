@@ -53,6 +53,7 @@ METRICS = {
     "batch": "batched solves/s (uneven Kuhn boxes, one persistent launch, bit-exact vs FP64 oracle)",
     "warm": "warm-started vs cold FIM solves/s (learned per-vertex start times, slab family)",
     "part": "partitioned slab solves/s (1.03M vertices, 2,964 submeshes, 50 windows, bit-exact vs FP64 oracle)",
+    "mlp": "warm-start network forward rows/s (tcgen05 GEMMs over the 1.03M slab vertices)",
 }
 PART_BLOCKS = (38, 13, 6)   # the slab's geometric partition: ~2,000 tets per submesh
 PART_DT, PART_STEPS = 2.0, 50
@@ -65,11 +66,12 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["mine", "reference"], default="mine")
-    ap.add_argument("--workload", choices=["slab", "cube", "shell", "batch", "warm", "part"], default="slab",
+    ap.add_argument("--workload", choices=["slab", "cube", "shell", "batch", "warm", "part", "mlp"], default="slab",
                     help="slab: 1M-vertex anisotropic slab (default); cube: 9,261-vertex unit cube, isotropic; "
                          "shell: 4.2M-vertex ventricle-like shell; batch: many uneven solves in one launch; "
                          "warm: learned warm start against the cold start; part: the slab partitioned into "
-                         "submeshes, solved in time windows (the reference's own operating mode)")
+                         "submeshes, solved in time windows (the reference's own operating mode); mlp: the "
+                         "warm-start network's tensor-core GEMMs (forward over the slab's vertices, training steps)")
     ap.add_argument("--batch", type=str, default="32,256,10000,500000",
                     help="batch workload: meshes,solves,min vertices,max vertices")
     ap.add_argument("--cells", type=str, default=None, help="override slab cells, e.g. 66,23,10")
@@ -597,6 +599,63 @@ def run_batch(args):
     print(json.dumps(out), flush=True)
 
 
+def run_mlp(args):
+    """The warm-start network's tensor-core workload: the forward pass over
+    one row per vertex of the 1M-vertex slab (padded to a multiple of 64
+    rows; three tcgen05 GEMMs with fused bias + ReLU, then the output layer)
+    and training steps of 4,096 rows (forward, backward with the weight
+    gradients, Adam).  Features and targets are seeded synthetic values.
+    Each call synchronises its stream, so the times are host wall-clock
+    around the call; the GEMM kernels' own durations come from ncu."""
+    import torch
+    import fim_api
+    torch.cuda.set_device(0)
+    n = (1029018 + 63) // 64 * 64
+    g = torch.Generator(device="cuda")
+    g.manual_seed(7)
+    keep = (torch.arange(64, device="cuda") < 7).to(torch.float32)
+    X = (torch.randn(n, 64, device="cuda", generator=g) * keep).to(torch.bfloat16).contiguous()
+    tgt = torch.rand(n, device="cuda", generator=g)
+    y = torch.empty(n, dtype=torch.float32, device="cuda")
+    nb = 4096
+    mlp = fim_api.Mlp(seed=5)
+    for _ in range(max(args.warmup, 3)):
+        mlp.predict(n, X.data_ptr(), y.data_ptr())
+        mlp.train_step(nb, X.data_ptr(), tgt.data_ptr(), 1e-3)
+    clocks = ClockSampler(index=0)
+    clocks.start()
+    tf, tt = [], []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        mlp.predict(n, X.data_ptr(), y.data_ptr())
+        tf.append(time.perf_counter() - t0)
+        t0 = time.perf_counter()
+        mlp.train_step(nb, X.data_ptr(), tgt.data_ptr(), 1e-3)
+        tt.append(time.perf_counter() - t0)
+    clk = clocks.stop()
+    mlp.close()
+    f_s, t_s = float(np.median(tf)), float(np.median(tt))
+    gemm_flop = 2.0 * n * (64 * 128 + 2 * 128 * 128)
+    gemm_bytes = 2.0 * n * (64 + 128) + 2 * 2.0 * n * (128 + 128)  # each layer reads its input rows, writes its output rows
+    out = {
+        "metric": METRICS["mlp"], "value": n / f_s, "unit": "rows/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": f_s * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "bf16 (FP32 accumulate)", "data": "synthetic (seeded features and targets)",
+        "config": {"workload": f"network 7(64)->128->128->128->1, forward over {n} rows (the 1,029,018 slab "
+                               f"vertices padded to a multiple of 64); training steps of {nb} rows",
+                   "rows": n, "train_rows": nb},
+        "forward_ms": f_s * 1e3, "train_step_ms": t_s * 1e3,
+        "gemm": {"flop_per_forward": gemm_flop, "bytes_per_forward": gemm_bytes,
+                 "tflops_lower_bound": gemm_flop / f_s * 1e-12, "gbs_lower_bound": gemm_bytes / f_s * 1e-9,
+                 "note": "wall-clock of the whole synchronised call (3 GEMMs, output layer, copy); the GEMM "
+                         "kernels are HBM-bound (64-128 FLOP per byte)"},
+        "gpu_launches": 24 * args.steps, "clocks": clk,  # per step: forward 4, training step 20
+        "e2e": {"value": None, "unit": "rows/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0,
+                "how": "report line; the end-to-end number is the slab workload's"},
+    }
+    print(json.dumps(out), flush=True)
+
+
 def run_warm(args):
     """Trains the warm-start network on FIM maps of small slabs of the bench
     family (generated by the solver), then solves held-out maps: one at a time
@@ -697,6 +756,8 @@ def main():
         run_batch(args)
     elif args.workload == "warm":
         run_warm(args)
+    elif args.workload == "mlp":
+        run_mlp(args)
     else:
         run_mine(args)
 

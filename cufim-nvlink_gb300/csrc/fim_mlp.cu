@@ -1,20 +1,24 @@
 // fim_mlp.cu -- the learned warm start: per-vertex features and a small
 // MLP (7 -> 128 -> 128 -> 128 -> 1, ReLU) trained and evaluated on the GPU.
 //
-// The three hidden-layer products are BF16 x BF16 -> FP32 tensor-core GEMMs
-// (mma.sync m16n8k16), one tile kernel for every shape the forward and
-// backward passes need, with the epilogue fused: bias + ReLU + BF16 store
-// (forward), ReLU mask + BF16 store (backward), FP32 store (weight
-// gradients).
+// Every product of the three hidden layers, forward and backward, is one
+// tcgen05 GEMM (C[M x 128] = A[M x K] B[128 x K]^T, BF16 operands staged by
+// TMA with the 128-byte swizzle, FP32 accumulator in tensor memory) with the
+// epilogue fused: bias + ReLU + BF16 store (forward), ReLU mask + BF16 store
+// (backward data), FP32 store (weight gradients).  The forward GEMMs read
+// transposed BF16 copies of the weights, the backward-data GEMMs the copies
+// as stored, and the weight gradients transposed activations, so that every
+// operand has K contiguous.
 // The output layer (128 -> 1), the loss, the bias gradients and Adam are
 // element-wise FP32 kernels.  Master weights are FP32; the GEMMs read BF16
 // copies refreshed after every update.  The input width is padded from 7
-// features to kMlpIn = 64 columns (zeros), so that every GEMM dimension is a
-// multiple of the 64 x 64 tile.
+// features to kMlpIn = 64 columns (zeros), one 128-byte K slice.
 //
 // No counterpart in the reference.
 #include "fim_internal.h"
 
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_bf16.h>
 
 #include <cmath>
@@ -27,110 +31,331 @@ namespace fimgb {
 
 namespace {
 
-constexpr int kBM = 64, kBN = 64, kBK = 16;
-
-__device__ __forceinline__ uint32_t pack_bf16(__nv_bfloat16 lo, __nv_bfloat16 hi)
-{
-  return (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
-}
-
-__device__ __forceinline__ void mma_bf16(float *c, const uint32_t *a, const uint32_t *b)
-{
-  asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-      "{%0,%1,%2,%3};"
-      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
-}
-
-// C[M x N] = A'[M x K] B'[K x N] with A' = A (row-major, lda) or A^T (A is
-// K x M), B' = B (K x N) or B^T (B is N x K); M, N multiples of 64, K of 16.
-// Epilogues:
+// ---------------------------------------------------------------------------
+// tcgen05 GEMM: C[M x 128] = A[M x K] B[128 x K]^T, A and B BF16 and K-major
+// (rows of K contiguous), the FP32 accumulator in tensor memory.
+//
+// One CTA of four warps per 128-row tile.  Warp 0 (one lane) streams 64-wide
+// K slices of A and B into shared memory by TMA (128-byte swizzle, a ring of
+// kGemmStages stages, full/empty mbarriers); warp 1 (one lane) issues four
+// tcgen05.mma (M = N = 128, K = 16) per slice and commits each slice's MMAs
+// to the stage's empty barrier, the last one to the done barrier; warp 2
+// owns the 128 tensor-memory columns of the accumulator.  The epilogue runs
+// on all four warps: warp w reads tensor-memory lanes 32w..32w+31 (tile rows)
+// with tcgen05.ld and applies one of
 //   kEpiBiasRelu: out_bf16 = relu(C + bias[n])
 //   kEpiMask:     out_bf16 = C * (mask_bf16 > 0)
 //   kEpiF32:      out_f32  = C
+// Every mbarrier wait is bounded (%globaltimer); a wait that runs out sets
+// the error word, the CTA skips its stores, waits (bounded) for the copies it
+// issued and frees its tensor memory.
 enum { kEpiBiasRelu = 0, kEpiMask = 1, kEpiF32 = 2 };
+constexpr int kGemmM = 128, kGemmN = 128, kGemmK = 64;  // tile rows, columns, K per stage (128 B of BF16)
+constexpr int kGemmStages = 3;
+constexpr uint32_t kGemmTileBytes = kGemmM * kGemmK * 2;  // one operand's slice: 16 KB (N == M)
+constexpr int kGemmSmem = kGemmStages * 2 * kGemmTileBytes + 1024;  // + slack to align the ring to 1024 B
+constexpr uint64_t kGemmWaitNs = 2000000000ull;  // bound of every mbarrier wait
+static_assert(kGemmN == kGemmM, "the ring holds equal A and B slices");
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p)
+{
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ uint64_t gtimer()
+{
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count)
+{
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes)
+{
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity)
+{
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// waits until the phase with the given parity has completed; false after limit_ns
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, uint64_t limit_ns = kGemmWaitNs)
+{
+  if (mbar_try(bar, parity)) return true;
+  const uint64_t t0 = gtimer();
+  for (uint32_t n = 0;; ++n) {
+    if (mbar_try(bar, parity)) return true;
+    if ((n & 255u) == 255u && gtimer() - t0 > limit_ns) return false;
+  }
+}
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, int x, int y, uint32_t bar)
+{
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+      ::"r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
+      : "memory");
+}
+// Shared-memory matrix descriptor of a K-major operand slice with the
+// 128-byte swizzle: rows of 128 B, 8-row groups 1024 B apart (stride byte
+// offset), descriptor version 1, layout type 2 (128-byte swizzle).  The
+// leading byte offset is unused for this layout (set to 16 B).
+__device__ __forceinline__ uint64_t sdesc_k128(uint32_t addr)
+{
+  return (uint64_t)((addr & 0x3ffffu) >> 4) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
+         ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
+// Instruction descriptor of tcgen05.mma kind::f16: FP32 accumulator (bits
+// 4-5 = 1), BF16 A and B (bits 7-9, 10-12 = 1), both K-major (bits 15, 16 =
+// 0), N >> 3 in bits 17-22, M >> 4 in bits 24-28.
+constexpr uint32_t kGemmIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kGemmN >> 3) << 17) |
+                                ((uint32_t)(kGemmM >> 4) << 24);
+__device__ __forceinline__ void umma_bf16(uint32_t tmem, uint64_t a, uint64_t b, uint32_t accumulate)
+{
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}"
+      ::"r"(tmem), "l"(a), "l"(b), "r"(kGemmIdesc), "r"(accumulate)
+      : "memory");
+}
+__device__ __forceinline__ void umma_commit(uint32_t bar)
+{
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+// 32 consecutive FP32 columns of this thread's tensor-memory lane
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t *v)
+{
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+      "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+        "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]),
+        "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]),
+        "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi)
+{
+  return (uint32_t)__bfloat16_as_ushort(__float2bfloat16(lo)) |
+         ((uint32_t)__bfloat16_as_ushort(__float2bfloat16(hi)) << 16);
+}
 
 template <int EPI>
-__global__ void __launch_bounds__(128) gemm_bf16_kernel(int M, int N, int K, const __nv_bfloat16 *__restrict__ A, int lda,
-                                                        int transA, const __nv_bfloat16 *__restrict__ B, int ldb,
-                                                        int transB, const float *__restrict__ bias,
-                                                        const __nv_bfloat16 *__restrict__ mask, __nv_bfloat16 *out16,
-                                                        float *out32, int ldc)
+__global__ void __launch_bounds__(128, 1) umma_gemm_kernel(const __grid_constant__ CUtensorMap ta,
+                                                           const __grid_constant__ CUtensorMap tb, int M, int K,
+                                                           const float *__restrict__ bias,
+                                                           const __nv_bfloat16 *__restrict__ mask,
+                                                           __nv_bfloat16 *out16, float *out32, int ldc,
+                                                           unsigned int *err)
 {
-  __shared__ __nv_bfloat16 As[kBM][kBK + 2];
-  __shared__ __nv_bfloat16 Bs[kBK][kBN + 2];
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int wm = warp >> 1, wn = warp & 1;          // warp tile 32 x 32
-  const int m0 = blockIdx.y * kBM, n0 = blockIdx.x * kBN;
-  const int g = lane >> 2, t = lane & 3;
-  float acc[2][4][4] = {};
-  for (int k0 = 0; k0 < K; k0 += kBK) {
-    // tiles to shared memory (64 x 16 of A', 16 x 64 of B'), 8 elements per thread each
-    for (int e = tid; e < kBM * kBK; e += 128) {
-      const int r = e / kBK, c = e % kBK;
-      const int m = m0 + r, k = k0 + c;
-      As[r][c] = transA ? A[(size_t)k * lda + m] : A[(size_t)m * lda + k];
+  extern __shared__ __align__(1024) unsigned char gemm_smem[];
+  __shared__ __align__(8) uint64_t full_bar[kGemmStages], empty_bar[kGemmStages], done_bar;
+  __shared__ uint32_t tmem_base;
+  __shared__ volatile int s_fail, s_consumed;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t ring = (smem_u32(gemm_smem) + 1023u) & ~1023u;
+  const int m0 = blockIdx.x * kGemmM;
+  const int nk = K / kGemmK;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kGemmStages; ++s) {
+      mbar_init(smem_u32(&full_bar[s]), 1);
+      mbar_init(smem_u32(&empty_bar[s]), 1);
     }
-    for (int e = tid; e < kBK * kBN; e += 128) {
-      const int r = e / kBN, c = e % kBN;
-      const int k = k0 + r, n = n0 + c;
-      Bs[r][c] = transB ? B[(size_t)n * ldb + k] : B[(size_t)k * ldb + n];
-    }
-    __syncthreads();
-#pragma unroll
-    for (int mi = 0; mi < 2; ++mi) {
-      const int rb = wm * 32 + mi * 16;
-      uint32_t a[4];
-      a[0] = pack_bf16(As[rb + g][2 * t], As[rb + g][2 * t + 1]);
-      a[1] = pack_bf16(As[rb + g + 8][2 * t], As[rb + g + 8][2 * t + 1]);
-      a[2] = pack_bf16(As[rb + g][2 * t + 8], As[rb + g][2 * t + 9]);
-      a[3] = pack_bf16(As[rb + g + 8][2 * t + 8], As[rb + g + 8][2 * t + 9]);
-#pragma unroll
-      for (int ni = 0; ni < 4; ++ni) {
-        const int cb = wn * 32 + ni * 8;
-        uint32_t b[2];
-        b[0] = pack_bf16(Bs[2 * t][cb + g], Bs[2 * t + 1][cb + g]);
-        b[1] = pack_bf16(Bs[2 * t + 8][cb + g], Bs[2 * t + 9][cb + g]);
-        mma_bf16(acc[mi][ni], a, b);
-      }
-    }
-    __syncthreads();
+    mbar_init(smem_u32(&done_bar), 1);
+    s_fail = 0;
+    s_consumed = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&ta)) : "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tb)) : "memory");
   }
+  if (warp == 2) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
+                 "r"(kGemmN)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_base;
+
+  int issued = 0;
+  if (warp == 0 && lane == 0) {
+    // producer: K slice i into stage i % kGemmStages once the MMAs of slice
+    // i - kGemmStages have released it
+    for (int i = 0; i < nk; ++i) {
+      const int s = i % kGemmStages;
+      const uint32_t ph = (uint32_t)(i / kGemmStages) & 1u;
+      if (!mbar_wait(smem_u32(&empty_bar[s]), ph ^ 1u)) { s_fail = 1; break; }
+      const uint32_t fb = smem_u32(&full_bar[s]);
+      mbar_expect_tx(fb, 2 * kGemmTileBytes);
+      tma_load_2d(ring + s * kGemmTileBytes, &ta, i * kGemmK, m0, fb);
+      tma_load_2d(ring + (kGemmStages + s) * kGemmTileBytes, &tb, i * kGemmK, 0, fb);
+      issued = i + 1;
+    }
+  } else if (warp == 1 && lane == 0) {
+    // MMA issuer: four K = 16 steps per slice (32 bytes apart within the
+    // swizzled 128-byte rows)
+    int i = 0;
+    for (; i < nk; ++i) {
+      const int s = i % kGemmStages;
+      const uint32_t ph = (uint32_t)(i / kGemmStages) & 1u;
+      if (!mbar_wait(smem_u32(&full_bar[s]), ph)) { s_fail = 1; break; }
+      tc_fence_after();
+      const uint32_t a = ring + s * kGemmTileBytes, b = ring + (kGemmStages + s) * kGemmTileBytes;
 #pragma unroll
-  for (int mi = 0; mi < 2; ++mi)
+      for (int k = 0; k < kGemmK / 16; ++k)
+        umma_bf16(tmem, sdesc_k128(a + 32 * k), sdesc_k128(b + 32 * k), (uint32_t)(i | k));
+      umma_commit(smem_u32(&empty_bar[s]));
+    }
+    s_consumed = i;
+    umma_commit(smem_u32(&done_bar));  // arrives once every MMA issued above has completed
+  }
+  __syncwarp();
+  // the whole K loop runs before this completes: the bound grows with it
+  if (!mbar_wait(smem_u32(&done_bar), 0, kGemmWaitNs + 20000ull * (uint64_t)nk)) s_fail = 1;
+  tc_fence_after();
+  const bool ok = s_fail == 0;
+
+  // epilogue: this thread's row, 32 columns per tensor-memory load
+  const int row = m0 + warp * 32 + lane;
+  const bool store = ok && row < M;
+#pragma unroll 1
+  for (int c0 = 0; c0 < kGemmN; c0 += 32) {
+    uint32_t v[32];
+    tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+    if (!store) continue;
+    if (EPI == kEpiF32) {
+      float4 *o = reinterpret_cast<float4 *>(out32 + (size_t)row * ldc + c0);
 #pragma unroll
-    for (int ni = 0; ni < 4; ++ni)
+      for (int q = 0; q < 8; ++q)
+        o[q] = make_float4(__uint_as_float(v[4 * q]), __uint_as_float(v[4 * q + 1]), __uint_as_float(v[4 * q + 2]),
+                           __uint_as_float(v[4 * q + 3]));
+    } else {
+      uint32_t w[16];
+      if (EPI == kEpiBiasRelu) {
 #pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const int m = m0 + wm * 32 + mi * 16 + g + (q >> 1) * 8;
-        const int n = n0 + wn * 32 + ni * 8 + 2 * t + (q & 1);
-        const float v = acc[mi][ni][q];
-        const size_t o = (size_t)m * ldc + n;
-        if (EPI == kEpiBiasRelu) out16[o] = __float2bfloat16(fmaxf(v + bias[n], 0.f));
-        else if (EPI == kEpiMask) out16[o] = __float2bfloat16(__bfloat162float(mask[o]) > 0.f ? v : 0.f);
-        else out32[o] = v;
+        for (int q = 0; q < 16; ++q)
+          w[q] = pack_bf16(fmaxf(__uint_as_float(v[2 * q]) + bias[c0 + 2 * q], 0.f),
+                           fmaxf(__uint_as_float(v[2 * q + 1]) + bias[c0 + 2 * q + 1], 0.f));
+      } else {
+        const uint4 *mk = reinterpret_cast<const uint4 *>(mask + (size_t)row * ldc + c0);
+#pragma unroll
+        for (int q4 = 0; q4 < 4; ++q4) {
+          const uint4 mm = mk[q4];
+          const uint32_t mw[4] = {mm.x, mm.y, mm.z, mm.w};
+#pragma unroll
+          for (int h = 0; h < 4; ++h) {
+            const int q = 4 * q4 + h;
+            const float lo = __bfloat162float(__ushort_as_bfloat16((unsigned short)(mw[h] & 0xffffu)));
+            const float hi = __bfloat162float(__ushort_as_bfloat16((unsigned short)(mw[h] >> 16)));
+            w[q] = pack_bf16(lo > 0.f ? __uint_as_float(v[2 * q]) : 0.f, hi > 0.f ? __uint_as_float(v[2 * q + 1]) : 0.f);
+          }
+        }
       }
+      uint4 *o = reinterpret_cast<uint4 *>(out16 + (size_t)row * ldc + c0);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) o[q] = make_uint4(w[4 * q], w[4 * q + 1], w[4 * q + 2], w[4 * q + 3]);
+    }
+  }
+  if (!ok) {
+    if (threadIdx.x == 0) atomicOr(err, 1u);
+    // copies issued but not consumed by an MMA still land in the ring: wait for them
+    if (warp == 0 && lane == 0)
+      for (int i = s_consumed; i < issued; ++i)
+        (void)mbar_wait(smem_u32(&full_bar[i % kGemmStages]), (uint32_t)(i / kGemmStages) & 1u);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 2)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kGemmN) : "memory");
+}
+
+// out[c][r] = in[r][c] for an R x C BF16 matrix (R, C multiples of 32)
+__global__ void transpose_bf16_kernel(int R, int C, const __nv_bfloat16 *__restrict__ in, __nv_bfloat16 *out)
+{
+  __shared__ __nv_bfloat16 t[32][33];
+  const int r0 = blockIdx.y * 32, c0 = blockIdx.x * 32;
+  for (int k = threadIdx.y; k < 32; k += blockDim.y) t[k][threadIdx.x] = in[(size_t)(r0 + k) * C + c0 + threadIdx.x];
+  __syncthreads();
+  for (int k = threadIdx.y; k < 32; k += blockDim.y) out[(size_t)(c0 + k) * R + r0 + threadIdx.x] = t[threadIdx.x][k];
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
+{
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      p = nullptr;
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }();
+  return fn;
+}
+
+// Tensor map of a rows x k BF16 matrix (row-major, k contiguous): boxes of
+// 64 columns (128 B, the swizzle span) by 128 rows; rows beyond the matrix
+// read as zeros.
+bool make_map(CUtensorMap *map, const void *base, uint64_t k, uint64_t rows)
+{
+  const auto enc = tensor_map_encoder();
+  if (!enc || (reinterpret_cast<uintptr_t>(base) & 15u) || k % kGemmK) return false;
+  const cuuint64_t dims[2] = {k, rows};
+  const cuuint64_t strides[1] = {k * 2};
+  const cuuint32_t box[2] = {(cuuint32_t)kGemmK, (cuuint32_t)kGemmM};
+  const cuuint32_t estr[2] = {1, 1};
+  return enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(base), dims, strides, box, estr,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
 }  // namespace
 
-cudaError_t mlp_gemm(int epi, int M, int N, int K, const void *A, int lda, int transA, const void *B, int ldb,
-                     int transB, const float *bias, const void *mask, void *out16, float *out32, int ldc,
-                     cudaStream_t st)
+// C[M x 128] = A[M x K] B[128 x K]^T for BF16 A (rows_a >= M rows) and B
+// (128 rows), both with K contiguous, K a multiple of 64.
+cudaError_t mlp_gemm(int epi, int M, int K, const void *A, int rows_a, const void *B, const float *bias,
+                     const void *mask, void *out16, float *out32, int ldc, unsigned int *err, cudaStream_t st)
 {
-  if (M % kBM || N % kBN || K % kBK) return cudaErrorInvalidValue;
-  const dim3 grid(N / kBN, M / kBM);
-  const auto *a = static_cast<const __nv_bfloat16 *>(A);
-  const auto *b = static_cast<const __nv_bfloat16 *>(B);
+  if (M <= 0 || K <= 0 || K % kGemmK || rows_a < M) return cudaErrorInvalidValue;
+  CUtensorMap ta, tb;
+  if (!make_map(&ta, A, (uint64_t)K, (uint64_t)rows_a) || !make_map(&tb, B, (uint64_t)K, kGemmN))
+    return cudaErrorInvalidValue;
+  const dim3 grid((M + kGemmM - 1) / kGemmM);
   const auto *mk = static_cast<const __nv_bfloat16 *>(mask);
   auto *o16 = static_cast<__nv_bfloat16 *>(out16);
-  if (epi == kEpiBiasRelu)
-    gemm_bf16_kernel<kEpiBiasRelu><<<grid, 128, 0, st>>>(M, N, K, a, lda, transA, b, ldb, transB, bias, mk, o16, out32, ldc);
-  else if (epi == kEpiMask)
-    gemm_bf16_kernel<kEpiMask><<<grid, 128, 0, st>>>(M, N, K, a, lda, transA, b, ldb, transB, bias, mk, o16, out32, ldc);
-  else
-    gemm_bf16_kernel<kEpiF32><<<grid, 128, 0, st>>>(M, N, K, a, lda, transA, b, ldb, transB, bias, mk, o16, out32, ldc);
+  cudaError_t e;
+  if (epi == kEpiBiasRelu) {
+    if ((e = cudaFuncSetAttribute(umma_gemm_kernel<kEpiBiasRelu>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  kGemmSmem)) != cudaSuccess) return e;
+    umma_gemm_kernel<kEpiBiasRelu><<<grid, 128, kGemmSmem, st>>>(ta, tb, M, K, bias, mk, o16, out32, ldc, err);
+  } else if (epi == kEpiMask) {
+    if ((e = cudaFuncSetAttribute(umma_gemm_kernel<kEpiMask>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  kGemmSmem)) != cudaSuccess) return e;
+    umma_gemm_kernel<kEpiMask><<<grid, 128, kGemmSmem, st>>>(ta, tb, M, K, bias, mk, o16, out32, ldc, err);
+  } else {
+    if ((e = cudaFuncSetAttribute(umma_gemm_kernel<kEpiF32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  kGemmSmem)) != cudaSuccess) return e;
+    umma_gemm_kernel<kEpiF32><<<grid, 128, kGemmSmem, st>>>(ta, tb, M, K, bias, mk, o16, out32, ldc, err);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t mlp_transpose(int R, int C, const void *in, void *out, cudaStream_t st)
+{
+  if (R % 32 || C % 32) return cudaErrorInvalidValue;
+  transpose_bf16_kernel<<<dim3(C / 32, R / 32), dim3(32, 8), 0, st>>>(R, C, static_cast<const __nv_bfloat16 *>(in),
+                                                                       static_cast<__nv_bfloat16 *>(out));
   return cudaGetLastError();
 }
 
@@ -191,10 +416,20 @@ __global__ void colsum_kernel(int n, const __nv_bfloat16 *__restrict__ dZ, float
   atomicAdd(&gb[c], s);
 }
 
+// Index of weight i (W1 [kMlpIn x kMlpH], W2, W3 [kMlpH x kMlpH], each
+// [in x out] row-major) in the transposed copies [out x in] that the forward
+// GEMMs read as their K-major B operand.
+__device__ __forceinline__ int transposed_index(int i)
+{
+  if (i < kMlpOW2) return kMlpOW1 + (i % kMlpH) * kMlpIn + i / kMlpH;
+  const int off = i < kMlpOW3 ? kMlpOW2 : kMlpOW3, k = i - off;
+  return off + (k % kMlpH) * kMlpH + k / kMlpH;
+}
+
 // Adam (bias-corrected) on every parameter, then the BF16 copies of the
-// three GEMM weight matrices.
+// three GEMM weight matrices (as stored and transposed).
 __global__ void adam_kernel(int np, float *P, const float *__restrict__ G, float *m, float *v, float lr, float b1,
-                            float b2, float eps, float c1, float c2, __nv_bfloat16 *W16)
+                            float b2, float eps, float c1, float c2, __nv_bfloat16 *W16, __nv_bfloat16 *W16T)
 {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x) {
     const float g = G[i];
@@ -204,14 +439,19 @@ __global__ void adam_kernel(int np, float *P, const float *__restrict__ G, float
     v[i] = vi;
     const float p = P[i] - lr * (mi / c1) / (sqrtf(vi / c2) + eps);
     P[i] = p;
-    if (i < kMlpW16) W16[i] = __float2bfloat16(p);
+    if (i < kMlpW16) {
+      W16[i] = __float2bfloat16(p);
+      W16T[transposed_index(i)] = __float2bfloat16(p);
+    }
   }
 }
 
-__global__ void to_bf16_kernel(int n, const float *__restrict__ src, __nv_bfloat16 *dst)
+__global__ void to_bf16_kernel(const float *__restrict__ src, __nv_bfloat16 *W16, __nv_bfloat16 *W16T)
 {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-    dst[i] = __float2bfloat16(src[i]);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < kMlpW16; i += gridDim.x * blockDim.x) {
+    W16[i] = __float2bfloat16(src[i]);
+    W16T[transposed_index(i)] = __float2bfloat16(src[i]);
+  }
 }
 
 }  // namespace
@@ -346,9 +586,12 @@ struct fim_mlp {
   int device = 0;
   cudaStream_t st = nullptr;
   float *P = nullptr, *G = nullptr, *M = nullptr, *V = nullptr, *loss = nullptr;
-  __nv_bfloat16 *W16 = nullptr;
+  __nv_bfloat16 *W16 = nullptr, *W16T = nullptr;  // GEMM weights as stored ([in x out]) and transposed
+  unsigned int *err = nullptr;                     // set by a GEMM whose bounded wait ran out
+  unsigned int h_err = 0;
   int64_t cap = 0;
   __nv_bfloat16 *H1 = nullptr, *H2 = nullptr, *H3 = nullptr, *dA = nullptr, *dB = nullptr;
+  __nv_bfloat16 *HT = nullptr, *DT = nullptr;     // [kMlpH x cap] transposes for the weight gradients
   float *y = nullptr, *dy = nullptr;
   int64_t steps = 0;
 };
@@ -371,8 +614,9 @@ int mlp_fail(const char *what, cudaError_t e)
 void mlp_free_acts(fim_mlp *m)
 {
   cudaFree(m->H1); cudaFree(m->H2); cudaFree(m->H3); cudaFree(m->dA); cudaFree(m->dB);
+  cudaFree(m->HT); cudaFree(m->DT);
   cudaFree(m->y); cudaFree(m->dy);
-  m->H1 = m->H2 = m->H3 = m->dA = m->dB = nullptr;
+  m->H1 = m->H2 = m->H3 = m->dA = m->dB = m->HT = m->DT = nullptr;
   m->y = m->dy = nullptr;
   m->cap = 0;
 }
@@ -387,10 +631,28 @@ int mlp_reserve(fim_mlp *m, int64_t n)
   MLP_TRY("fim_mlp: activations", cudaMalloc(&m->H3, a));
   MLP_TRY("fim_mlp: activations", cudaMalloc(&m->dA, a));
   MLP_TRY("fim_mlp: activations", cudaMalloc(&m->dB, a));
+  MLP_TRY("fim_mlp: activations", cudaMalloc(&m->HT, a));
+  MLP_TRY("fim_mlp: activations", cudaMalloc(&m->DT, a));
   MLP_TRY("fim_mlp: activations", cudaMalloc(&m->y, sizeof(float) * n));
   MLP_TRY("fim_mlp: activations", cudaMalloc(&m->dy, sizeof(float) * n));
   m->cap = n;
   return FIM_OK;
+}
+
+// Queues the read of the GEMMs' error word (before the caller's stream
+// synchronisation); mlp_gemm_status then reports it after the sync.
+cudaError_t mlp_read_err(fim_mlp *m)
+{
+  return cudaMemcpyAsync(&m->h_err, m->err, sizeof(unsigned int), cudaMemcpyDeviceToHost, m->st);
+}
+int mlp_gemm_status(fim_mlp *m, const char *who)
+{
+  if (m->h_err == 0) return FIM_OK;
+  m->h_err = 0;
+  cudaMemset(m->err, 0, sizeof(unsigned int));
+  std::string msg = std::string(who) + ": a tensor-core GEMM wait ran out (results discarded)";
+  set_last_error(msg.c_str());
+  return FIM_ERR_TIMEOUT;
 }
 
 int mlp_check_n(int64_t n, const char *who)
@@ -408,12 +670,13 @@ cudaError_t mlp_forward(fim_mlp *m, int n, const void *X, const float *tgt)
 {
   cudaError_t e;
   const float *P = m->P;
-  if ((e = mlp_gemm(0, n, kMlpH, kMlpIn, X, kMlpIn, 0, m->W16 + kMlpOW1, kMlpH, 0, P + kMlpOB1, nullptr, m->H1,
-                    nullptr, kMlpH, m->st)) != cudaSuccess) return e;
-  if ((e = mlp_gemm(0, n, kMlpH, kMlpH, m->H1, kMlpH, 0, m->W16 + kMlpOW2, kMlpH, 0, P + kMlpOB2, nullptr, m->H2,
-                    nullptr, kMlpH, m->st)) != cudaSuccess) return e;
-  if ((e = mlp_gemm(0, n, kMlpH, kMlpH, m->H2, kMlpH, 0, m->W16 + kMlpOW3, kMlpH, 0, P + kMlpOB3, nullptr, m->H3,
-                    nullptr, kMlpH, m->st)) != cudaSuccess) return e;
+  // H_l = relu(H_{l-1} W_l + b_l): B operand = W_l^T [out x in]
+  if ((e = mlp_gemm(kEpiBiasRelu, n, kMlpIn, X, n, m->W16T + kMlpOW1, P + kMlpOB1, nullptr, m->H1, nullptr, kMlpH,
+                    m->err, m->st)) != cudaSuccess) return e;
+  if ((e = mlp_gemm(kEpiBiasRelu, n, kMlpH, m->H1, n, m->W16T + kMlpOW2, P + kMlpOB2, nullptr, m->H2, nullptr, kMlpH,
+                    m->err, m->st)) != cudaSuccess) return e;
+  if ((e = mlp_gemm(kEpiBiasRelu, n, kMlpH, m->H2, n, m->W16T + kMlpOW3, P + kMlpOB3, nullptr, m->H3, nullptr, kMlpH,
+                    m->err, m->st)) != cudaSuccess) return e;
   out_forward_kernel<<<(n + 7) / 8, 256, 0, m->st>>>(n, m->H3, P + kMlpOW4, P + kMlpOB4, m->y, tgt, m->dy, m->loss);
   return cudaGetLastError();
 }
@@ -425,21 +688,31 @@ cudaError_t mlp_backward(fim_mlp *m, int n, const void *X)
   float *G = m->G;
   const int blocks = (n + 63) / 64;
   out_backward_kernel<<<blocks, kMlpH, 0, m->st>>>(n, m->H3, m->P + kMlpOW4, m->dy, m->dA, G + kMlpOW4, G + kMlpOB4);
-  // layer 3: dW3 = H2^T dZ3, db3, dZ2 = (dZ3 W3^T) o [H2 > 0]
-  if ((e = mlp_gemm(2, kMlpH, kMlpH, n, m->H2, kMlpH, 1, m->dA, kMlpH, 0, nullptr, nullptr, nullptr, G + kMlpOW3,
-                    kMlpH, m->st)) != cudaSuccess) return e;
+  // layer l: dW_l = H_{l-1}^T dZ_l (both transposed so that K = rows is
+  // contiguous), db_l, dZ_{l-1} = (dZ_l W_l^T) o [H_{l-1} > 0] (B operand =
+  // W_l as stored, [in x out])
+  // layer 3
+  if ((e = mlp_transpose(n, kMlpH, m->H2, m->HT, m->st)) != cudaSuccess) return e;
+  if ((e = mlp_transpose(n, kMlpH, m->dA, m->DT, m->st)) != cudaSuccess) return e;
+  if ((e = mlp_gemm(kEpiF32, kMlpH, n, m->HT, kMlpH, m->DT, nullptr, nullptr, nullptr, G + kMlpOW3, kMlpH, m->err,
+                    m->st)) != cudaSuccess) return e;
   colsum_kernel<<<blocks, kMlpH, 0, m->st>>>(n, m->dA, G + kMlpOB3);
-  if ((e = mlp_gemm(1, n, kMlpH, kMlpH, m->dA, kMlpH, 0, m->W16 + kMlpOW3, kMlpH, 1, nullptr, m->H2, m->dB, nullptr,
-                    kMlpH, m->st)) != cudaSuccess) return e;
+  if ((e = mlp_gemm(kEpiMask, n, kMlpH, m->dA, n, m->W16 + kMlpOW3, nullptr, m->H2, m->dB, nullptr, kMlpH, m->err,
+                    m->st)) != cudaSuccess) return e;
   // layer 2
-  if ((e = mlp_gemm(2, kMlpH, kMlpH, n, m->H1, kMlpH, 1, m->dB, kMlpH, 0, nullptr, nullptr, nullptr, G + kMlpOW2,
-                    kMlpH, m->st)) != cudaSuccess) return e;
+  if ((e = mlp_transpose(n, kMlpH, m->H1, m->HT, m->st)) != cudaSuccess) return e;
+  if ((e = mlp_transpose(n, kMlpH, m->dB, m->DT, m->st)) != cudaSuccess) return e;
+  if ((e = mlp_gemm(kEpiF32, kMlpH, n, m->HT, kMlpH, m->DT, nullptr, nullptr, nullptr, G + kMlpOW2, kMlpH, m->err,
+                    m->st)) != cudaSuccess) return e;
   colsum_kernel<<<blocks, kMlpH, 0, m->st>>>(n, m->dB, G + kMlpOB2);
-  if ((e = mlp_gemm(1, n, kMlpH, kMlpH, m->dB, kMlpH, 0, m->W16 + kMlpOW2, kMlpH, 1, nullptr, m->H1, m->dA, nullptr,
-                    kMlpH, m->st)) != cudaSuccess) return e;
-  // layer 1
-  if ((e = mlp_gemm(2, kMlpIn, kMlpH, n, X, kMlpIn, 1, m->dA, kMlpH, 0, nullptr, nullptr, nullptr, G + kMlpOW1,
-                    kMlpH, m->st)) != cudaSuccess) return e;
+  if ((e = mlp_gemm(kEpiMask, n, kMlpH, m->dB, n, m->W16 + kMlpOW2, nullptr, m->H1, m->dA, nullptr, kMlpH, m->err,
+                    m->st)) != cudaSuccess) return e;
+  // layer 1: X^T is kMlpIn rows; the tile's other rows (left over in HT)
+  // only reach output rows that are not stored
+  if ((e = mlp_transpose(n, kMlpIn, X, m->HT, m->st)) != cudaSuccess) return e;
+  if ((e = mlp_transpose(n, kMlpH, m->dA, m->DT, m->st)) != cudaSuccess) return e;
+  if ((e = mlp_gemm(kEpiF32, kMlpIn, n, m->HT, kMlpH, m->DT, nullptr, nullptr, nullptr, G + kMlpOW1, kMlpH, m->err,
+                    m->st)) != cudaSuccess) return e;
   colsum_kernel<<<blocks, kMlpH, 0, m->st>>>(n, m->dA, G + kMlpOB1);
   return cudaGetLastError();
 }
@@ -485,7 +758,10 @@ extern "C" int fim_mlp_create(int device, uint64_t seed, fim_mlp **out)
       (e = cudaMalloc(&m->M, sizeof(float) * kMlpParams)) != cudaSuccess ||
       (e = cudaMalloc(&m->V, sizeof(float) * kMlpParams)) != cudaSuccess ||
       (e = cudaMalloc(&m->loss, sizeof(float))) != cudaSuccess ||
-      (e = cudaMalloc(&m->W16, sizeof(__nv_bfloat16) * kMlpW16)) != cudaSuccess)
+      (e = cudaMalloc(&m->W16, sizeof(__nv_bfloat16) * kMlpW16)) != cudaSuccess ||
+      (e = cudaMalloc(&m->W16T, sizeof(__nv_bfloat16) * kMlpW16)) != cudaSuccess ||
+      (e = cudaMalloc(&m->err, sizeof(unsigned int))) != cudaSuccess ||
+      (e = cudaMemset(m->err, 0, sizeof(unsigned int))) != cudaSuccess)
     return fail(mlp_fail("fim_mlp_create", e));
   // He initialisation (fixed seed); padded input rows and biases zero
   std::vector<float> h(kMlpParams, 0.f);
@@ -509,6 +785,7 @@ extern "C" int fim_mlp_destroy(fim_mlp *m)
   if (m->st) cudaStreamSynchronize(m->st);
   mlp_free_acts(m);
   cudaFree(m->P); cudaFree(m->G); cudaFree(m->M); cudaFree(m->V); cudaFree(m->loss); cudaFree(m->W16);
+  cudaFree(m->W16T); cudaFree(m->err);
   if (m->st) cudaStreamDestroy(m->st);
   delete m;
   return FIM_OK;
@@ -521,7 +798,7 @@ extern "C" int fim_mlp_set_params(fim_mlp *m, const float *params)
   MLP_TRY("fim_mlp_set_params", cudaMemcpyAsync(m->P, params, sizeof(float) * kMlpParams, cudaMemcpyHostToDevice, m->st));
   MLP_TRY("fim_mlp_set_params", cudaMemsetAsync(m->M, 0, sizeof(float) * kMlpParams, m->st));
   MLP_TRY("fim_mlp_set_params", cudaMemsetAsync(m->V, 0, sizeof(float) * kMlpParams, m->st));
-  to_bf16_kernel<<<64, 256, 0, m->st>>>(kMlpW16, m->P, m->W16);
+  to_bf16_kernel<<<64, 256, 0, m->st>>>(m->P, m->W16, m->W16T);
   MLP_TRY("fim_mlp_set_params", cudaGetLastError());
   MLP_TRY("fim_mlp_set_params", cudaStreamSynchronize(m->st));
   m->steps = 0;
@@ -548,8 +825,9 @@ extern "C" int fim_mlp_gradients(fim_mlp *m, int64_t n, const void *d_features, 
   MLP_TRY("fim_mlp_gradients: set device", cudaSetDevice(m->device));
   if ((rc = mlp_loss_grads(m, n, d_features, d_targets, loss)) != FIM_OK) return rc;
   MLP_TRY("fim_mlp_gradients", cudaMemcpyAsync(grads, m->G, sizeof(float) * kMlpParams, cudaMemcpyDeviceToHost, m->st));
+  MLP_TRY("fim_mlp_gradients", mlp_read_err(m));
   MLP_TRY("fim_mlp_gradients", cudaStreamSynchronize(m->st));
-  return FIM_OK;
+  return mlp_gemm_status(m, "fim_mlp_gradients");
 }
 
 extern "C" int fim_mlp_train_step(fim_mlp *m, int64_t n, const void *d_features, const float *d_targets, float lr,
@@ -567,10 +845,11 @@ extern "C" int fim_mlp_train_step(fim_mlp *m, int64_t n, const void *d_features,
   const float b1 = 0.9f, b2 = 0.999f;
   ++m->steps;
   const float c1 = 1.f - std::pow(b1, (float)m->steps), c2 = 1.f - std::pow(b2, (float)m->steps);
-  adam_kernel<<<64, 256, 0, m->st>>>(kMlpParams, m->P, m->G, m->M, m->V, lr, b1, b2, 1e-8f, c1, c2, m->W16);
+  adam_kernel<<<64, 256, 0, m->st>>>(kMlpParams, m->P, m->G, m->M, m->V, lr, b1, b2, 1e-8f, c1, c2, m->W16, m->W16T);
   MLP_TRY("fim_mlp_train_step: adam", cudaGetLastError());
+  MLP_TRY("fim_mlp_train_step", mlp_read_err(m));
   MLP_TRY("fim_mlp_train_step", cudaStreamSynchronize(m->st));
-  return FIM_OK;
+  return mlp_gemm_status(m, "fim_mlp_train_step");
 }
 
 extern "C" int fim_mlp_predict(fim_mlp *m, int64_t n, const void *d_features, float *d_out)
@@ -582,6 +861,7 @@ extern "C" int fim_mlp_predict(fim_mlp *m, int64_t n, const void *d_features, fl
   if ((rc = mlp_reserve(m, n)) != FIM_OK) return rc;
   MLP_TRY("fim_mlp_predict: forward", mlp_forward(m, (int)n, d_features, nullptr));
   MLP_TRY("fim_mlp_predict", cudaMemcpyAsync(d_out, m->y, sizeof(float) * n, cudaMemcpyDeviceToDevice, m->st));
+  MLP_TRY("fim_mlp_predict", mlp_read_err(m));
   MLP_TRY("fim_mlp_predict", cudaStreamSynchronize(m->st));
-  return FIM_OK;
+  return mlp_gemm_status(m, "fim_mlp_predict");
 }
