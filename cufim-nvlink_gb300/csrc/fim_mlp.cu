@@ -21,6 +21,7 @@
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <random>
@@ -32,24 +33,23 @@ namespace fimgb {
 namespace {
 
 // ---------------------------------------------------------------------------
-// tcgen05 GEMM: C[M x 128] = A[M x K] B[128 x K]^T, A and B BF16 and K-major
-// (rows of K contiguous), the FP32 accumulator in tensor memory.
+// tcgen05 GEMMs: C[M x 128] = A[M x K] B[128 x K]^T, A and B BF16 and
+// K-major (rows of K contiguous), the FP32 accumulator in tensor memory.
+// Operands are staged by TMA as 64-wide K slices (128 bytes, the swizzle
+// span) with the 128-byte swizzle, and every mbarrier wait is bounded
+// (%globaltimer): a wait that runs out sets the error word, the CTA skips
+// its stores, waits (bounded) for the copies and MMAs it issued and frees
+// its tensor memory.
 //
-// One CTA of four warps per 128-row tile.  Warp 0 (one lane) streams 64-wide
-// K slices of A and B into shared memory by TMA (128-byte swizzle, a ring of
-// kGemmStages stages, full/empty mbarriers); warp 1 (one lane) issues four
-// tcgen05.mma (M = N = 128, K = 16) per slice and commits each slice's MMAs
-// to the stage's empty barrier, the last one to the done barrier; warp 2
-// owns the 128 tensor-memory columns of the accumulator.  The epilogue runs
-// on all four warps: warp w reads tensor-memory lanes 32w..32w+31 (tile rows)
-// with tcgen05.ld and applies one of
-//   kEpiBiasRelu: out_bf16 = relu(C + bias[n])
-//   kEpiMask:     out_bf16 = C * (mask_bf16 > 0)
-//   kEpiF32:      out_f32  = C
-// Every mbarrier wait is bounded (%globaltimer); a wait that runs out sets
-// the error word, the CTA skips its stores, waits (bounded) for the copies it
-// issued and frees its tensor memory.
-enum { kEpiBiasRelu = 0, kEpiMask = 1, kEpiF32 = 2 };
+// umma_gemm_kernel (the weight gradients: M <= 128, long K): one CTA of four
+// warps per 128-row tile.  Warp 0 (one lane) streams the K slices of A and B
+// through a ring of kGemmStages stages (full/empty mbarriers); warp 1 (one
+// lane) issues four tcgen05.mma (M = N = 128, K = 16) per slice and commits
+// each slice's MMAs to the stage's empty barrier, the last one to the done
+// barrier; warp 2 owns the 128 tensor-memory columns of the accumulator; all
+// four warps then read it back (warp w: lanes 32w..32w+31, the tile rows)
+// with tcgen05.ld and store FP32.
+enum { kEpiBiasRelu = 0, kEpiMask = 1 };
 constexpr int kGemmM = 128, kGemmN = 128, kGemmK = 64;  // tile rows, columns, K per stage (128 B of BF16)
 constexpr int kGemmStages = 3;
 constexpr uint32_t kGemmTileBytes = kGemmM * kGemmK * 2;  // one operand's slice: 16 KB (N == M)
@@ -102,6 +102,14 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map
       ::"r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
       : "memory");
 }
+__device__ __forceinline__ void tma_store_2d(const CUtensorMap *map, uint32_t src, int x, int y)
+{
+  asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%2, %3}], [%1];"
+               ::"l"(reinterpret_cast<uint64_t>(map)), "r"(src), "r"(x), "r"(y)
+               : "memory");
+  asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+}
+
 // Shared-memory matrix descriptor of a K-major operand slice with the
 // 128-byte swizzle: rows of 128 B, 8-row groups 1024 B apart (stride byte
 // offset), descriptor version 1, layout type 2 (128-byte swizzle).  The
@@ -130,8 +138,9 @@ __device__ __forceinline__ void umma_commit(uint32_t bar)
 }
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-// 32 consecutive FP32 columns of this thread's tensor-memory lane
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t *v)
+// 32 consecutive FP32 columns of this thread's tensor-memory lane (issued;
+// tmem_wait_ld makes them readable)
+__device__ __forceinline__ void tmem_ld32_issue(uint32_t taddr, uint32_t *v)
 {
   asm volatile(
       "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
@@ -141,7 +150,12 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t *v)
         "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]),
         "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
       : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t *v)
+{
+  tmem_ld32_issue(taddr, v);
+  tmem_wait_ld();
 }
 
 __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi)
@@ -150,13 +164,9 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi)
          ((uint32_t)__bfloat16_as_ushort(__float2bfloat16(hi)) << 16);
 }
 
-template <int EPI>
 __global__ void __launch_bounds__(128, 1) umma_gemm_kernel(const __grid_constant__ CUtensorMap ta,
                                                            const __grid_constant__ CUtensorMap tb, int M, int K,
-                                                           const float *__restrict__ bias,
-                                                           const __nv_bfloat16 *__restrict__ mask,
-                                                           __nv_bfloat16 *out16, float *out32, int ldc,
-                                                           unsigned int *err)
+                                                           float *out32, int ldc, unsigned int *err)
 {
   extern __shared__ __align__(1024) unsigned char gemm_smem[];
   __shared__ __align__(8) uint64_t full_bar[kGemmStages], empty_bar[kGemmStages], done_bar;
@@ -235,38 +245,11 @@ __global__ void __launch_bounds__(128, 1) umma_gemm_kernel(const __grid_constant
     uint32_t v[32];
     tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
     if (!store) continue;
-    if (EPI == kEpiF32) {
-      float4 *o = reinterpret_cast<float4 *>(out32 + (size_t)row * ldc + c0);
+    float4 *o = reinterpret_cast<float4 *>(out32 + (size_t)row * ldc + c0);
 #pragma unroll
-      for (int q = 0; q < 8; ++q)
-        o[q] = make_float4(__uint_as_float(v[4 * q]), __uint_as_float(v[4 * q + 1]), __uint_as_float(v[4 * q + 2]),
-                           __uint_as_float(v[4 * q + 3]));
-    } else {
-      uint32_t w[16];
-      if (EPI == kEpiBiasRelu) {
-#pragma unroll
-        for (int q = 0; q < 16; ++q)
-          w[q] = pack_bf16(fmaxf(__uint_as_float(v[2 * q]) + bias[c0 + 2 * q], 0.f),
-                           fmaxf(__uint_as_float(v[2 * q + 1]) + bias[c0 + 2 * q + 1], 0.f));
-      } else {
-        const uint4 *mk = reinterpret_cast<const uint4 *>(mask + (size_t)row * ldc + c0);
-#pragma unroll
-        for (int q4 = 0; q4 < 4; ++q4) {
-          const uint4 mm = mk[q4];
-          const uint32_t mw[4] = {mm.x, mm.y, mm.z, mm.w};
-#pragma unroll
-          for (int h = 0; h < 4; ++h) {
-            const int q = 4 * q4 + h;
-            const float lo = __bfloat162float(__ushort_as_bfloat16((unsigned short)(mw[h] & 0xffffu)));
-            const float hi = __bfloat162float(__ushort_as_bfloat16((unsigned short)(mw[h] >> 16)));
-            w[q] = pack_bf16(lo > 0.f ? __uint_as_float(v[2 * q]) : 0.f, hi > 0.f ? __uint_as_float(v[2 * q + 1]) : 0.f);
-          }
-        }
-      }
-      uint4 *o = reinterpret_cast<uint4 *>(out16 + (size_t)row * ldc + c0);
-#pragma unroll
-      for (int q = 0; q < 4; ++q) o[q] = make_uint4(w[4 * q], w[4 * q + 1], w[4 * q + 2], w[4 * q + 3]);
-    }
+    for (int q = 0; q < 8; ++q)
+      o[q] = make_float4(__uint_as_float(v[4 * q]), __uint_as_float(v[4 * q + 1]), __uint_as_float(v[4 * q + 2]),
+                         __uint_as_float(v[4 * q + 3]));
   }
   if (!ok) {
     if (threadIdx.x == 0) atomicOr(err, 1u);
@@ -279,6 +262,258 @@ __global__ void __launch_bounds__(128, 1) umma_gemm_kernel(const __grid_constant
   __syncthreads();
   if (warp == 2)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kGemmN) : "memory");
+}
+
+// ---------------------------------------------------------------------------
+// Persistent row-tile GEMM for the tall products (M = rows, K = 64 or 128):
+// C[M x 128] = A[M x K] W[128 x K]^T, one CTA per SM looping over 128-row
+// tiles.  The weights (B) are loaded once per CTA; warp 0 streams A tiles
+// through a ring of kRowStages stages; warp 1 issues the MMAs of tile j into
+// tensor-memory accumulator j % 2; warps 2-9 drain accumulator j % 2 (warp w
+// reads lanes 32 (w % 4) .. +31, the tile rows, and columns 64 h .. 64 h + 63
+// with h = (w - 2) / 4) while the MMAs of tile j + 1 run, release it (tempty)
+// and then apply the epilogue:
+//   kEpiBiasRelu:    out_bf16 = relu(C + bias)
+//   kEpiMask:        out_bf16 = C * (mask_bf16 > 0)
+//   kEpiBiasReluOut: h = bf16(relu(C + bias)) (stored when out_bf16 is set),
+//                    y = h . w4 + b4 (the output layer), and with targets
+//                    dy = 2 (y - t) / M and the summed squared error; the
+//                    warps of columns 64..127 hand their partial dot
+//                    products to those of columns 0..63 through shared
+//                    memory (mbarrier ypart), which add them in a fixed
+//                    order and release the accumulator after reading them.
+enum { kEpiBiasReluOut = 3 };
+constexpr int kRowStages = 3;
+constexpr int kRowKMax = 128, kRowSlices = kRowKMax / kGemmK;
+constexpr uint32_t kRowStageBytes = kRowSlices * kGemmTileBytes;     // one A tile (32 KB)
+constexpr uint32_t kRowStgBytes = 32 * kGemmK * 2;  // one epilogue warp's 32 x 64 output box (4 KB)
+constexpr int kRowEpiWarps = 8;
+// B + the A ring + two output boxes per epilogue warp + alignment slack
+constexpr int kRowSmem = (1 + kRowStages) * kRowStageBytes + 2 * kRowEpiWarps * kRowStgBytes + 1024;
+constexpr int kRowThreads = 320;  // producer, MMA issuer, 8 epilogue warps
+
+template <int EPI>
+__global__ void __launch_bounds__(kRowThreads, 1) umma_rows_kernel(
+    const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb,
+    const __grid_constant__ CUtensorMap to, int M, int K, const float *__restrict__ bias,
+    const __nv_bfloat16 *__restrict__ mask, int store, int ldc,
+    const float *__restrict__ w4, const float *__restrict__ b4, float *y, const float *__restrict__ tgt, float *dy,
+    float *loss, unsigned int *err)
+{
+  extern __shared__ __align__(1024) unsigned char gemm_smem[];
+  __shared__ __align__(8) uint64_t bfull, afull[kRowStages], aempty[kRowStages], tfull[2], tempty[2], ypart[2];
+  __shared__ float s_part[2][kGemmM];
+  __shared__ uint32_t tmem_base;
+  __shared__ float s_bias[kGemmN], s_w4[kGemmN];
+  __shared__ volatile int s_fail;
+  __shared__ int s_issued, s_consumed, s_mma_issued, s_drained;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t bsm = (smem_u32(gemm_smem) + 1023u) & ~1023u, aring = bsm + kRowStageBytes;
+  const uint32_t stg0 = aring + kRowStages * kRowStageBytes;  // output boxes: [warp - 2][tile parity]
+  const int nks = K / kGemmK;
+  const uint32_t tile_bytes = (uint32_t)nks * kGemmTileBytes;
+  const int ntiles = (M + kGemmM - 1) / kGemmM;
+  if (threadIdx.x == 0) {
+    mbar_init(smem_u32(&bfull), 1);
+    for (int s = 0; s < kRowStages; ++s) {
+      mbar_init(smem_u32(&afull[s]), 1);
+      mbar_init(smem_u32(&aempty[s]), 1);
+    }
+    for (int a = 0; a < 2; ++a) {
+      mbar_init(smem_u32(&tfull[a]), 1);
+      mbar_init(smem_u32(&tempty[a]), 8);  // one arrival per epilogue warp
+      mbar_init(smem_u32(&ypart[a]), 4);   // the warps of columns 64..127
+    }
+    s_fail = 0;
+    s_issued = s_consumed = s_mma_issued = s_drained = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&ta)) : "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tb)) : "memory");
+    if (store) asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&to)) : "memory");
+  }
+  if (threadIdx.x < kGemmN) {
+    s_bias[threadIdx.x] = (EPI == kEpiMask) ? 0.f : bias[threadIdx.x];
+    s_w4[threadIdx.x] = (EPI == kEpiBiasReluOut) ? w4[threadIdx.x] : 0.f;
+  }
+  if (warp == 2) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
+                 "r"(2 * kGemmN)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_base;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      // producer: the weights once, then A tile j into stage j % kRowStages
+      mbar_expect_tx(smem_u32(&bfull), tile_bytes);
+      for (int ks = 0; ks < nks; ++ks)
+        tma_load_2d(bsm + ks * kGemmTileBytes, &tb, ks * kGemmK, 0, smem_u32(&bfull));
+      int j = 0;
+      for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++j) {
+        const int s = j % kRowStages;
+        if (s_fail || !mbar_wait(smem_u32(&aempty[s]), ((uint32_t)(j / kRowStages) & 1u) ^ 1u)) { s_fail = 1; break; }
+        const uint32_t fb = smem_u32(&afull[s]);
+        mbar_expect_tx(fb, tile_bytes);
+        for (int ks = 0; ks < nks; ++ks)
+          tma_load_2d(aring + s * kRowStageBytes + ks * kGemmTileBytes, &ta, ks * kGemmK, tile * kGemmM, fb);
+        s_issued = j + 1;
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // MMA issuer: tile j into accumulator j % 2 once the epilogue has drained it
+      if (!mbar_wait(smem_u32(&bfull), 0)) s_fail = 1;
+      int j = 0;
+      for (int tile = blockIdx.x; tile < ntiles && !s_fail; tile += gridDim.x, ++j) {
+        const int s = j % kRowStages, acc = j & 1;
+        if (!mbar_wait(smem_u32(&tempty[acc]), ((uint32_t)(j >> 1) & 1u) ^ 1u) ||
+            !mbar_wait(smem_u32(&afull[s]), (uint32_t)(j / kRowStages) & 1u)) { s_fail = 1; break; }
+        tc_fence_after();
+        const uint32_t a = aring + s * kRowStageBytes, d = tmem + (uint32_t)(acc * kGemmN);
+        for (int ks = 0; ks < nks; ++ks)
+#pragma unroll
+          for (int k = 0; k < kGemmK / 16; ++k)
+            umma_bf16(d, sdesc_k128(a + ks * kGemmTileBytes + 32 * k), sdesc_k128(bsm + ks * kGemmTileBytes + 32 * k),
+                      (uint32_t)(ks | k));
+        umma_commit(smem_u32(&aempty[s]));
+        umma_commit(smem_u32(&tfull[acc]));
+        s_consumed = j + 1;
+        s_mma_issued = j + 1;
+      }
+    }
+  } else {
+    // epilogue warps 2..9: tensor-memory lanes 32 q .. 32 q + 31 (tile rows),
+    // columns cb .. cb + 63
+    const int q = warp & 3, h = (warp - 2) >> 2, cb = 64 * h;
+    auto release = [&](int acc, int j) {
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&tempty[acc])) : "memory");
+      if (warp == 2 && lane == 0) s_drained = j + 1;
+    };
+    int j = 0;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++j) {
+      const int acc = j & 1;
+      const uint32_t par = (uint32_t)(j >> 1) & 1u;
+      if (s_fail || !mbar_wait(smem_u32(&tfull[acc]), par)) { s_fail = 1; break; }
+      tc_fence_after();
+      const int row = tile * kGemmM + q * 32 + lane;
+      const bool in = row < M;
+      uint32_t v[64];
+      const uint32_t tv = tmem + (uint32_t)(acc * kGemmN) + ((uint32_t)(q * 32) << 16) + (uint32_t)cb;
+      tmem_ld32_issue(tv, v);
+      tmem_ld32_issue(tv + 32, v + 32);
+      tmem_wait_ld();
+      const bool combine = EPI == kEpiBiasReluOut && h == 0;  // releases after reading the partials
+      if (!combine) release(acc, j);
+      // this warp's 32 x 64 output box goes through shared memory (128-byte
+      // swizzle: 16-byte chunk c of row r at chunk c ^ (r % 8)) and one TMA
+      // store, which clips the rows past M; first the store issued from the
+      // same buffer two tiles ago must have read it
+      const uint32_t stg = stg0 + (uint32_t)(((warp - 2) * 2 + (j & 1)) * kRowStgBytes);
+      if (store) {
+        if (lane == 0) asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
+        __syncwarp();
+      }
+      float ysum = 0.f;
+#pragma unroll
+      for (int c = 0; c < 64; c += 32) {
+        const int col = cb + c;
+        uint32_t w[16];
+        if (EPI == kEpiMask) {
+          const uint4 *mk = reinterpret_cast<const uint4 *>(mask + (size_t)row * ldc + col);
+#pragma unroll
+          for (int q4 = 0; q4 < 4; ++q4) {
+            const uint4 mm = in ? mk[q4] : make_uint4(0u, 0u, 0u, 0u);
+            const uint32_t mw[4] = {mm.x, mm.y, mm.z, mm.w};
+#pragma unroll
+            for (int hh = 0; hh < 4; ++hh) {
+              const int e = 4 * q4 + hh;
+              const float lo = __bfloat162float(__ushort_as_bfloat16((unsigned short)(mw[hh] & 0xffffu)));
+              const float hi = __bfloat162float(__ushort_as_bfloat16((unsigned short)(mw[hh] >> 16)));
+              w[e] = pack_bf16(lo > 0.f ? __uint_as_float(v[c + 2 * e]) : 0.f,
+                               hi > 0.f ? __uint_as_float(v[c + 2 * e + 1]) : 0.f);
+            }
+          }
+        } else {
+#pragma unroll
+          for (int e = 0; e < 16; ++e) {
+            w[e] = pack_bf16(fmaxf(__uint_as_float(v[c + 2 * e]) + s_bias[col + 2 * e], 0.f),
+                             fmaxf(__uint_as_float(v[c + 2 * e + 1]) + s_bias[col + 2 * e + 1], 0.f));
+            if (EPI == kEpiBiasReluOut) {  // the output layer on the stored (BF16) activations
+              ysum += __bfloat162float(__ushort_as_bfloat16((unsigned short)(w[e] & 0xffffu))) * s_w4[col + 2 * e];
+              ysum += __bfloat162float(__ushort_as_bfloat16((unsigned short)(w[e] >> 16))) * s_w4[col + 2 * e + 1];
+            }
+          }
+        }
+        if (store) {
+#pragma unroll
+          for (int k4 = 0; k4 < 4; ++k4) {
+            const uint32_t chunk = (uint32_t)((c >> 3) + k4) ^ (uint32_t)(lane & 7);
+            const uint32_t a = stg + (uint32_t)lane * 128u + chunk * 16u;
+            asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(a), "r"(w[4 * k4]), "r"(w[4 * k4 + 1]),
+                         "r"(w[4 * k4 + 2]), "r"(w[4 * k4 + 3])
+                         : "memory");
+          }
+        }
+      }
+      if (store) {
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncwarp();
+        if (lane == 0) tma_store_2d(&to, stg, cb, tile * kGemmM + q * 32);
+      }
+      if (EPI == kEpiBiasReluOut) {
+        if (h == 1) {  // hand the partial dot product over
+          s_part[acc][q * 32 + lane] = ysum;
+          __syncwarp();
+          if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&ypart[acc])) : "memory");
+        } else {
+          const bool okp = mbar_wait(smem_u32(&ypart[acc]), par);
+          if (!okp) s_fail = 1;
+          const float p1 = s_part[acc][q * 32 + lane];
+          release(acc, j);
+          float se = 0.f;
+          if (okp && in) {
+            const float yv = (ysum + p1) + b4[0];
+            y[row] = yv;
+            if (tgt) {
+              const float e = yv - tgt[row];
+              dy[row] = 2.f * e / (float)M;
+              se = e * e;
+            }
+          }
+          if (tgt) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) se += __shfl_xor_sync(0xffffffffu, se, o);
+            if (lane == 0) atomicAdd(loss, se);
+          }
+        }
+      }
+    }
+    if (store && lane == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");  // the output is written
+  }
+  __syncthreads();
+  if (s_fail) {
+    if (threadIdx.x == 0) {
+      atomicOr(err, 1u);
+      // the weights, copies issued but not consumed, MMAs issued but not
+      // drained: let them land (bounded)
+      (void)mbar_wait(smem_u32(&bfull), 0);
+      for (int j = s_consumed; j < s_issued; ++j)
+        (void)mbar_wait(smem_u32(&afull[j % kRowStages]), (uint32_t)(j / kRowStages) & 1u);
+      for (int j = s_drained; j < s_mma_issued; ++j)
+        (void)mbar_wait(smem_u32(&tfull[j & 1]), (uint32_t)(j >> 1) & 1u);
+    }
+    __syncthreads();
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 2)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * kGemmN) : "memory");
 }
 
 // out[c][r] = in[r][c] for an R x C BF16 matrix (R, C multiples of 32)
@@ -307,13 +542,13 @@ PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
 // Tensor map of a rows x k BF16 matrix (row-major, k contiguous): boxes of
 // 64 columns (128 B, the swizzle span) by 128 rows; rows beyond the matrix
 // read as zeros.
-bool make_map(CUtensorMap *map, const void *base, uint64_t k, uint64_t rows)
+bool make_map(CUtensorMap *map, const void *base, uint64_t k, uint64_t rows, uint32_t box_rows = kGemmM)
 {
   const auto enc = tensor_map_encoder();
   if (!enc || (reinterpret_cast<uintptr_t>(base) & 15u) || k % kGemmK) return false;
   const cuuint64_t dims[2] = {k, rows};
   const cuuint64_t strides[1] = {k * 2};
-  const cuuint32_t box[2] = {(cuuint32_t)kGemmK, (cuuint32_t)kGemmM};
+  const cuuint32_t box[2] = {(cuuint32_t)kGemmK, box_rows};
   const cuuint32_t estr[2] = {1, 1};
   return enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(base), dims, strides, box, estr,
              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
@@ -322,32 +557,66 @@ bool make_map(CUtensorMap *map, const void *base, uint64_t k, uint64_t rows)
 
 }  // namespace
 
-// C[M x 128] = A[M x K] B[128 x K]^T for BF16 A (rows_a >= M rows) and B
-// (128 rows), both with K contiguous, K a multiple of 64.
-cudaError_t mlp_gemm(int epi, int M, int K, const void *A, int rows_a, const void *B, const float *bias,
-                     const void *mask, void *out16, float *out32, int ldc, unsigned int *err, cudaStream_t st)
+// Weight gradients: C[M x 128] = A[M x K] B[128 x K]^T (FP32 out) for BF16
+// A (rows_a >= M rows) and B (128 rows), both with K contiguous, K a
+// multiple of 64 (the K loop of umma_gemm_kernel).
+cudaError_t mlp_gemm_wgrad(int M, int K, const void *A, int rows_a, const void *B, float *out32, int ldc,
+                           unsigned int *err, cudaStream_t st)
 {
   if (M <= 0 || K <= 0 || K % kGemmK || rows_a < M) return cudaErrorInvalidValue;
   CUtensorMap ta, tb;
   if (!make_map(&ta, A, (uint64_t)K, (uint64_t)rows_a) || !make_map(&tb, B, (uint64_t)K, kGemmN))
     return cudaErrorInvalidValue;
-  const dim3 grid((M + kGemmM - 1) / kGemmM);
-  const auto *mk = static_cast<const __nv_bfloat16 *>(mask);
-  auto *o16 = static_cast<__nv_bfloat16 *>(out16);
   cudaError_t e;
-  if (epi == kEpiBiasRelu) {
-    if ((e = cudaFuncSetAttribute(umma_gemm_kernel<kEpiBiasRelu>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  kGemmSmem)) != cudaSuccess) return e;
-    umma_gemm_kernel<kEpiBiasRelu><<<grid, 128, kGemmSmem, st>>>(ta, tb, M, K, bias, mk, o16, out32, ldc, err);
-  } else if (epi == kEpiMask) {
-    if ((e = cudaFuncSetAttribute(umma_gemm_kernel<kEpiMask>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  kGemmSmem)) != cudaSuccess) return e;
-    umma_gemm_kernel<kEpiMask><<<grid, 128, kGemmSmem, st>>>(ta, tb, M, K, bias, mk, o16, out32, ldc, err);
-  } else {
-    if ((e = cudaFuncSetAttribute(umma_gemm_kernel<kEpiF32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  kGemmSmem)) != cudaSuccess) return e;
-    umma_gemm_kernel<kEpiF32><<<grid, 128, kGemmSmem, st>>>(ta, tb, M, K, bias, mk, o16, out32, ldc, err);
-  }
+  if ((e = cudaFuncSetAttribute(umma_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kGemmSmem)) !=
+      cudaSuccess) return e;
+  umma_gemm_kernel<<<dim3((M + kGemmM - 1) / kGemmM), 128, kGemmSmem, st>>>(ta, tb, M, K, out32, ldc, err);
+  return cudaGetLastError();
+}
+
+// The tall products: C[M x 128] = A[M x K] W[128 x K]^T with K = 64 or 128
+// (umma_rows_kernel, one CTA per SM); epilogue arguments as the kernel's.
+struct RowEpi {
+  const float *bias = nullptr;
+  const void *mask = nullptr;
+  void *out16 = nullptr;
+  const float *w4 = nullptr, *b4 = nullptr;
+  float *y = nullptr;
+  const float *tgt = nullptr;
+  float *dy = nullptr, *loss = nullptr;
+};
+
+cudaError_t mlp_gemm_rows(int epi, int M, int K, const void *A, const void *W, const RowEpi &x, unsigned int *err,
+                          cudaStream_t st)
+{
+  if (M <= 0 || (K != 64 && K != 128)) return cudaErrorInvalidValue;
+  CUtensorMap ta, tb;
+  CUtensorMap to;  // the output in 32 x 64 boxes (unused without a BF16 output)
+  const int store = x.out16 != nullptr;
+  if (!make_map(&ta, A, (uint64_t)K, (uint64_t)M) || !make_map(&tb, W, (uint64_t)K, kGemmN))
+    return cudaErrorInvalidValue;
+  if (!store) to = ta;
+  else if (!make_map(&to, x.out16, kGemmN, (uint64_t)M, 32)) return cudaErrorInvalidValue;
+  int dev = 0, nsm = 0;
+  cudaError_t e;
+  if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+  if ((e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+  const int ntiles = (M + kGemmM - 1) / kGemmM;
+  const dim3 grid(std::min(ntiles, nsm));
+  const auto *mk = static_cast<const __nv_bfloat16 *>(x.mask);
+#define FIM_ROWS_LAUNCH(E)                                                                                           \
+  do {                                                                                                              \
+    if ((e = cudaFuncSetAttribute(umma_rows_kernel<E>, cudaFuncAttributeMaxDynamicSharedMemorySize, kRowSmem)) !=   \
+        cudaSuccess)                                                                                                \
+      return e;                                                                                                     \
+    umma_rows_kernel<E><<<grid, kRowThreads, kRowSmem, st>>>(ta, tb, to, M, K, x.bias, mk, store, kGemmN, x.w4, x.b4, \
+                                                             x.y, x.tgt, x.dy, x.loss, err);                       \
+  } while (0)
+  if (epi == kEpiBiasRelu) FIM_ROWS_LAUNCH(kEpiBiasRelu);
+  else if (epi == kEpiMask) FIM_ROWS_LAUNCH(kEpiMask);
+  else if (epi == kEpiBiasReluOut) FIM_ROWS_LAUNCH(kEpiBiasReluOut);
+  else return cudaErrorInvalidValue;
+#undef FIM_ROWS_LAUNCH
   return cudaGetLastError();
 }
 
@@ -363,30 +632,6 @@ cudaError_t mlp_transpose(int R, int C, const void *in, void *out, cudaStream_t 
 // element-wise parts of the network
 
 namespace {
-
-// y[r] = H3[r] . w4 + b4 (FP32 over the BF16 activations); with targets, the
-// squared error is summed into loss and dy[r] = 2 (y - t) / n.
-__global__ void out_forward_kernel(int n, const __nv_bfloat16 *__restrict__ H3, const float *__restrict__ w4,
-                                   const float *__restrict__ b4, float *y, const float *__restrict__ tgt, float *dy,
-                                   float *loss)
-{
-  const int lane = threadIdx.x & 31;
-  const int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  if (r >= n) return;
-  float s = 0.f;
-  for (int c = lane; c < kMlpH; c += 32) s += __bfloat162float(H3[(size_t)r * kMlpH + c]) * w4[c];
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-  s += b4[0];
-  if (lane == 0) {
-    y[r] = s;
-    if (tgt) {
-      const float e = s - tgt[r];
-      dy[r] = 2.f * e / (float)n;
-      atomicAdd(loss, e * e);
-    }
-  }
-}
 
 // dZ3[r][c] = bf16(dy[r] w4[c]) where H3 > 0; gw4[c] += sum_r H3[r][c] dy[r];
 // gb4 += sum_r dy[r].  One block per 64 rows, one thread per column.
@@ -670,14 +915,18 @@ cudaError_t mlp_forward(fim_mlp *m, int n, const void *X, const float *tgt)
 {
   cudaError_t e;
   const float *P = m->P;
-  // H_l = relu(H_{l-1} W_l + b_l): B operand = W_l^T [out x in]
-  if ((e = mlp_gemm(kEpiBiasRelu, n, kMlpIn, X, n, m->W16T + kMlpOW1, P + kMlpOB1, nullptr, m->H1, nullptr, kMlpH,
-                    m->err, m->st)) != cudaSuccess) return e;
-  if ((e = mlp_gemm(kEpiBiasRelu, n, kMlpH, m->H1, n, m->W16T + kMlpOW2, P + kMlpOB2, nullptr, m->H2, nullptr, kMlpH,
-                    m->err, m->st)) != cudaSuccess) return e;
-  if ((e = mlp_gemm(kEpiBiasRelu, n, kMlpH, m->H2, n, m->W16T + kMlpOW3, P + kMlpOB3, nullptr, m->H3, nullptr, kMlpH,
-                    m->err, m->st)) != cudaSuccess) return e;
-  out_forward_kernel<<<(n + 7) / 8, 256, 0, m->st>>>(n, m->H3, P + kMlpOW4, P + kMlpOB4, m->y, tgt, m->dy, m->loss);
+  // H_l = relu(H_{l-1} W_l + b_l): B operand = W_l^T [out x in]; the last
+  // layer's epilogue also evaluates the output layer (and, with targets,
+  // dy and the loss); H3 is stored only for the backward pass
+  RowEpi x1, x2, x3;
+  x1.bias = P + kMlpOB1; x1.out16 = m->H1;
+  x2.bias = P + kMlpOB2; x2.out16 = m->H2;
+  x3.bias = P + kMlpOB3; x3.out16 = tgt ? m->H3 : nullptr;
+  x3.w4 = P + kMlpOW4; x3.b4 = P + kMlpOB4; x3.y = m->y; x3.tgt = tgt; x3.dy = m->dy; x3.loss = m->loss;
+  if ((e = mlp_gemm_rows(kEpiBiasRelu, n, kMlpIn, X, m->W16T + kMlpOW1, x1, m->err, m->st)) != cudaSuccess) return e;
+  if ((e = mlp_gemm_rows(kEpiBiasRelu, n, kMlpH, m->H1, m->W16T + kMlpOW2, x2, m->err, m->st)) != cudaSuccess) return e;
+  if ((e = mlp_gemm_rows(kEpiBiasReluOut, n, kMlpH, m->H2, m->W16T + kMlpOW3, x3, m->err, m->st)) != cudaSuccess)
+    return e;
   return cudaGetLastError();
 }
 
@@ -694,25 +943,23 @@ cudaError_t mlp_backward(fim_mlp *m, int n, const void *X)
   // layer 3
   if ((e = mlp_transpose(n, kMlpH, m->H2, m->HT, m->st)) != cudaSuccess) return e;
   if ((e = mlp_transpose(n, kMlpH, m->dA, m->DT, m->st)) != cudaSuccess) return e;
-  if ((e = mlp_gemm(kEpiF32, kMlpH, n, m->HT, kMlpH, m->DT, nullptr, nullptr, nullptr, G + kMlpOW3, kMlpH, m->err,
-                    m->st)) != cudaSuccess) return e;
+  if ((e = mlp_gemm_wgrad(kMlpH, n, m->HT, kMlpH, m->DT, G + kMlpOW3, kMlpH, m->err, m->st)) != cudaSuccess) return e;
   colsum_kernel<<<blocks, kMlpH, 0, m->st>>>(n, m->dA, G + kMlpOB3);
-  if ((e = mlp_gemm(kEpiMask, n, kMlpH, m->dA, n, m->W16 + kMlpOW3, nullptr, m->H2, m->dB, nullptr, kMlpH, m->err,
-                    m->st)) != cudaSuccess) return e;
+  RowEpi xm;
+  xm.mask = m->H2; xm.out16 = m->dB;
+  if ((e = mlp_gemm_rows(kEpiMask, n, kMlpH, m->dA, m->W16 + kMlpOW3, xm, m->err, m->st)) != cudaSuccess) return e;
   // layer 2
   if ((e = mlp_transpose(n, kMlpH, m->H1, m->HT, m->st)) != cudaSuccess) return e;
   if ((e = mlp_transpose(n, kMlpH, m->dB, m->DT, m->st)) != cudaSuccess) return e;
-  if ((e = mlp_gemm(kEpiF32, kMlpH, n, m->HT, kMlpH, m->DT, nullptr, nullptr, nullptr, G + kMlpOW2, kMlpH, m->err,
-                    m->st)) != cudaSuccess) return e;
+  if ((e = mlp_gemm_wgrad(kMlpH, n, m->HT, kMlpH, m->DT, G + kMlpOW2, kMlpH, m->err, m->st)) != cudaSuccess) return e;
   colsum_kernel<<<blocks, kMlpH, 0, m->st>>>(n, m->dB, G + kMlpOB2);
-  if ((e = mlp_gemm(kEpiMask, n, kMlpH, m->dB, n, m->W16 + kMlpOW2, nullptr, m->H1, m->dA, nullptr, kMlpH, m->err,
-                    m->st)) != cudaSuccess) return e;
+  xm.mask = m->H1; xm.out16 = m->dA;
+  if ((e = mlp_gemm_rows(kEpiMask, n, kMlpH, m->dB, m->W16 + kMlpOW2, xm, m->err, m->st)) != cudaSuccess) return e;
   // layer 1: X^T is kMlpIn rows; the tile's other rows (left over in HT)
   // only reach output rows that are not stored
   if ((e = mlp_transpose(n, kMlpIn, X, m->HT, m->st)) != cudaSuccess) return e;
   if ((e = mlp_transpose(n, kMlpH, m->dA, m->DT, m->st)) != cudaSuccess) return e;
-  if ((e = mlp_gemm(kEpiF32, kMlpIn, n, m->HT, kMlpH, m->DT, nullptr, nullptr, nullptr, G + kMlpOW1, kMlpH, m->err,
-                    m->st)) != cudaSuccess) return e;
+  if ((e = mlp_gemm_wgrad(kMlpIn, n, m->HT, kMlpH, m->DT, G + kMlpOW1, kMlpH, m->err, m->st)) != cudaSuccess) return e;
   colsum_kernel<<<blocks, kMlpH, 0, m->st>>>(n, m->dA, G + kMlpOB1);
   return cudaGetLastError();
 }
