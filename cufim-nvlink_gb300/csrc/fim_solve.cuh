@@ -401,12 +401,6 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
   constexpr bool kMarkedMode = is_marked_mode(MODE);
   const double *ph = MODE == kMarked2 ? d.phi2 : d.phi;      // times this phase reads
   const float *phf = MODE == kMarked2 ? d.phi2_f : d.phi_f;
-#ifndef FIM_APER
-#define FIM_APER 1
-#endif
-  // corners per thread and round in phase A: one (12.44 ms on the 1M slab)
-  // beats the hand-batched loads of two (12.55) and three (12.92)
-  constexpr int kPer = FIM_APER;
   const int tid = threadIdx.x, lane = tid & 31;
   const int64_t per_block = lo_.local ? (int64_t)n : ((int64_t)n + gridDim.x - 1) / gridDim.x;
   const int64_t lbeg = lo_.local ? 0 : min((int64_t)n, (int64_t)blockIdx.x * per_block);
@@ -458,95 +452,76 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
       if (tid == 0) sh.nslot = max(1, fit);
     }
     __syncthreads();
-    PROBE(kPrSetup);
     const int nslot = sh.nslot;
     const int total = sh.cp[nslot];     // may exceed kCornerCap for a single huge vertex
     const int kept = min(total, kCornerCap);
+    // the slot of every corner of the batch, so that phase A issues each
+    // record load without searching the corner prefix first
+    if (tid < nslot) {
+      const int j1 = min(sh.cp[tid + 1], kept);
+      for (int j = sh.cp[tid]; j < j1; ++j) sh.cs[j] = (uint8_t)tid;
+    }
+    __syncthreads();
+    PROBE(kPrSetup);
 
-    // A: load, validity, float edge bounds.  Pass 1 loads every corner's
-    // first-read record (ids, float lengths, fp16 bounds), pass 2 the
-    // neighbours' states and float times; within a pass the loads of a
-    // thread's corners are independent, so they are all in flight together.
-    for (int jb = 0; jb < kept; jb += kPer * kThreads) {
-      // all of a thread's record loads first, then the neighbour loads that
-      // need their ids, then the stores: every load of a pass is in flight
-      // at once
-      int slot[kPer];
-      uint4 h0[kPer], h1[kPer];
-#pragma unroll
-      for (int r = 0; r < kPer; ++r) {
-        const int j = jb + tid + r * kThreads;
-        slot[r] = 0;
-        h0[r] = make_uint4(0u, 0u, 0u, 0u);
-        h1[r] = h0[r];
-        if (j < kept) {
-          int lo = 0, hi = nslot - 1;  // last slot with cp[slot] <= j
-          while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (sh.cp[mid] <= j) lo = mid; else hi = mid - 1;
-          }
-          slot[r] = lo;
-          const int64_t c = sh.c0[lo] + (j - sh.cp[lo]);
-          h0[r] = __ldg(d.crec + kCrecWords * c);
-          h1[r] = __ldg(d.crec + kCrecWords * c + 1);
-        }
+    // A: load, validity, float edge bounds.  Every thread walks its corners
+    // j = tid, tid + kThreads, ...: the first-read record (ids, float
+    // lengths, fp16 bounds) of the next corner is loaded while the
+    // neighbours' states and float times of the current one are (they need
+    // its ids), so that a thread's corners are not a chain of round trips.
+    {
+      uint4 n0 = make_uint4(0u, 0u, 0u, 0u), n1 = n0;
+      if (tid < kept) {
+        const int sl = sh.cs[tid];
+        const int64_t c = sh.c0[sl] + (tid - sh.cp[sl]);
+        n0 = __ldg(d.crec + kCrecWords * c);
+        n1 = __ldg(d.crec + kCrecWords * c + 1);
       }
-      float pf[kPer][3];
-      uint8_t stn[kPer][3];
-#pragma unroll
-      for (int r = 0; r < kPer; ++r) {
-        const int j = jb + tid + r * kThreads;
-        if (j < kept) {
-          const int32_t nbs[3] = {(int32_t)h0[r].x, (int32_t)h0[r].y, (int32_t)h0[r].z};
-#pragma unroll
-          for (int i = 0; i < 3; ++i) {
-            pf[r][i] = __ldcg(phf + nbs[i]);
-            stn[r][i] = (uint8_t)sw_seen(__ldcg(d.sw + nbs[i]), kMarkedMode, stamp);
-          }
+      for (int j = tid; j < kept; j += kThreads) {
+        const uint4 h0 = n0, h1 = n1;
+        const int slot = sh.cs[j];
+        const int jn = j + kThreads;
+        if (jn < kept) {  // prefetch the next corner's record
+          const int sl = sh.cs[jn];
+          const int64_t c = sh.c0[sl] + (jn - sh.cp[sl]);
+          n0 = __ldg(d.crec + kCrecWords * c);
+          n1 = __ldg(d.crec + kCrecWords * c + 1);
         }
-      }
+        float pf[3];
+        uint8_t stn[3];
+        const int32_t nbs[3] = {(int32_t)h0.x, (int32_t)h0.y, (int32_t)h0.z};
 #pragma unroll
-      for (int r = 0; r < kPer; ++r) {
-        const int j = jb + tid + r * kThreads;
-        if (j < kept) {
-          sh.hb[j][0] = h0[r].w;
-          sh.hb[j][1] = h1[r].w;
-          sh.sf[j][0] = __uint_as_float(h1[r].x); sh.sf[j][1] = __uint_as_float(h1[r].y);
-          sh.sf[j][2] = __uint_as_float(h1[r].z);
-          sh.cs[j] = (uint8_t)slot[r];
+        for (int i = 0; i < 3; ++i) {
+          pf[i] = __ldcg(phf + nbs[i]);
+          stn[i] = (uint8_t)sw_seen(__ldcg(d.sw + nbs[i]), kMarkedMode, stamp);
         }
-      }
-#pragma unroll
-      for (int r = 0; r < kPer; ++r) {
-        const int j = jb + tid + r * kThreads;
-        if (j >= kept) continue;
+        sh.hb[j][0] = h0.w;
+        sh.hb[j][1] = h1.w;
+        const float len[3] = {__uint_as_float(h1.x), __uint_as_float(h1.y), __uint_as_float(h1.z)};
         uint32_t m = 0;
         float ub = INFINITY;
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
-          const Re P = re_in(pf[r][i]);
-          bool ok = stn[r][i] >= ST_NARROW;
+          const Re P = re_in(pf[i]);
+          bool ok = stn[i] >= ST_NARROW;
           if (ok) {
             if (re_lo(P) > lower_hi) ok = true;
             else if (re_hi(P) <= lower_lo) ok = false;
-            else {  // rare: the FP64 time decides
-              int32_t nb[3];
-              corner_nb(d, sh.c0[slot[r]] + (j - sh.cp[slot[r]]), nb);
-              ok = __ldcg(ph + pick3(nb, i)) > lower;
-            }
+            else ok = __ldcg(ph + nbs[i]) > lower;  // rare: the FP64 time decides
           }
           if (ok) {
             m |= 1u << i;
-            const Re E = P + re_len(sh.sf[j][i]);
+            const Re E = P + re_len(len[i]);
             ub = fminf(ub, re_hi(E));
-            if (!fp32) sh.sf[j][i] = re_lo(E);  // exact mode: the edge's lower bound replaces its length
-          } else if (!fp32) {
-            sh.sf[j][i] = INFINITY;
+            // exact mode: the edge's lower bound replaces its length
+            sh.sf[j][i] = fp32 ? len[i] : re_lo(E);
+          } else {
+            sh.sf[j][i] = fp32 ? len[i] : INFINITY;
           }
-          sh.pf[j][i] = pf[r][i];
+          sh.pf[j][i] = pf[i];
         }
         if (m) ++n_filtered;
-        if (!exact_all && ub < INFINITY) atomicMin(&sh.bhi[slot[r]], fkey(ub));
+        if (!exact_all && ub < INFINITY) atomicMin(&sh.bhi[slot], fkey(ub));
         sh.vm[j] = (uint8_t)m;
       }
     }
@@ -1341,14 +1316,24 @@ inline cudaError_t prepare(int device, int block, int *max_grid)
   return cudaSuccess;
 }
 
+// A cooperative launch (every block co-resident: the grid barrier relies on
+// it), through cudaLaunchKernelEx so that stream capture records it as a
+// cooperative kernel node.
 inline cudaError_t launch(const FimDev &d, const FimParams &p, int grid, int block, cudaStream_t stream)
 {
-  FimDev dd = d;
-  FimParams pp = p;
-  void *args[] = {&dd, &pp};
-  const void *fn = p.local ? (const void *)fim_solve_kernel<kPathLocal>
-                 : p.two_phase ? (const void *)fim_solve_kernel<kPathTwo> : (const void *)fim_solve_kernel<kPathFour>;
-  return cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(block), args, sizeof(BatchSh), stream);
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = sizeof(BatchSh);
+  cfg.stream = stream;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  if (p.local) return cudaLaunchKernelEx(&cfg, fim_solve_kernel<kPathLocal>, d, p);
+  if (p.two_phase) return cudaLaunchKernelEx(&cfg, fim_solve_kernel<kPathTwo>, d, p);
+  return cudaLaunchKernelEx(&cfg, fim_solve_kernel<kPathFour>, d, p);
 }
 
 }  // namespace FIM_SHAPE_NS

@@ -80,6 +80,14 @@ struct fim_solver {
   cudaStream_t own_stream = nullptr;  // created by fim_create (blocking: ordered after legacy-stream work)
   cudaStream_t stream = nullptr;      // working stream (own_stream unless fim_set_stream)
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // the persistent launch as a CUDA graph: captured on cap_stream, replayed
+  // while the launch's arguments (gd, gp) and configuration stay the same
+  cudaStream_t cap_stream = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  FimDev gd{};
+  FimParams gp{};
+  int gshape = -1, ggrid = 0, gblock = 0;
+  bool graph_ok = true;  // false once capture turned out to be unavailable
   // conduction upload: copy stream, one event per chunk (chunk copies
   // overlap the metric kernel of the chunk before), first invalid tet
   cudaStream_t copy_stream = nullptr;
@@ -247,6 +255,8 @@ extern "C" int fim_destroy(fim_solver *s)
   if (s->stream) cudaStreamSynchronize(s->stream);
   if (s->own_stream) cudaStreamSynchronize(s->own_stream);
   if (s->copy_stream) cudaStreamSynchronize(s->copy_stream);
+  if (s->gexec) cudaGraphExecDestroy(s->gexec);
+  if (s->cap_stream) cudaStreamDestroy(s->cap_stream);
   if (s->ev0) cudaEventDestroy(s->ev0);
   if (s->ev1) cudaEventDestroy(s->ev1);
   if (s->ev_dep) cudaEventDestroy(s->ev_dep);
@@ -707,7 +717,8 @@ static void block_ranges(const fim_solver *s, int grid, std::vector<int32_t> &ou
 // Launch parameters and device view of the solver's staged problem.
 static void solve_args(const fim_solver *s, FimDev &d, FimParams &p)
 {
-  d = FimDev{};
+  // zeroed bytewise (padding included): the graph cache compares them bytewise
+  std::memset(static_cast<void *>(&d), 0, sizeof d);
   d.nV = (int32_t)s->nL; d.nG = (int32_t)s->nV; d.nT = s->nT; d.nC = s->nC;
   d.gptr = s->gptr.p; d.gcopy = s->gcopy.p; d.phi_out = s->phi_out.p; d.st_out = s->st_out.p;
   d.cptr = s->cptr.p; d.crec = s->crec.p; d.cgeo = s->cgeo.p; d.cgf = s->cgf.p; d.nptr = s->nptr.p; d.nbr = s->nbr.p;
@@ -718,7 +729,7 @@ static void solve_args(const fim_solver *s, FimDev &d, FimParams &p)
   d.seed_v = s->seed_v.p; d.seed_t = s->seed_t.p; d.nseed = s->nseed;
   d.phi_init = s->warm;
   d.ctl = s->ctl.p;
-  p = FimParams{};
+  std::memset(static_cast<void *>(&p), 0, sizeof p);
   p.dt = s->opts.dt;
   p.n_steps = s->opts.n_steps;
   p.front_width = s->opts.front_width >= 0.0 ? s->opts.front_width : s->front_width;
@@ -728,6 +739,45 @@ static void solve_args(const fim_solver *s, FimDev &d, FimParams &p)
   p.exact_all = s->opts.exact_all ? 1 : 0;
   p.fp32 = (s->opts.fp32_update && !s->opts.exact_all) ? 1 : 0;
   p.two_phase = two_phase_ok(p) ? 1 : 0;
+}
+
+// The persistent launch as a CUDA graph: graph_prepare keeps the cached
+// graph when the kernel's arguments and configuration equal those it was
+// captured with, else captures the launch on cap_stream (thread-local mode,
+// so other threads' CUDA calls are not affected) and instantiates it; it
+// returns whether the graph can be launched.  Where capture or instantiation
+// fails the solver launches directly from then on.  It runs before the
+// solve's timing events, so capturing costs no measured device time.
+static bool graph_prepare(fim_solver *s, const FimDev &d, const FimParams &p, int shape, int grid, bool *captured)
+{
+  *captured = false;
+  if (!s->graph_ok) return false;
+  if (s->gexec && s->gshape == shape && s->ggrid == grid && s->gblock == s->block &&
+      std::memcmp(&s->gd, &d, sizeof d) == 0 && std::memcmp(&s->gp, &p, sizeof p) == 0)
+    return true;
+  if (s->gexec) { cudaGraphExecDestroy(s->gexec); s->gexec = nullptr; }
+  cudaError_t e = cudaSuccess;
+  if (!s->cap_stream) e = cudaStreamCreateWithFlags(&s->cap_stream, cudaStreamNonBlocking);
+  cudaGraph_t g = nullptr;
+  if (e == cudaSuccess) e = cudaStreamBeginCapture(s->cap_stream, cudaStreamCaptureModeThreadLocal);
+  if (e == cudaSuccess) {
+    const cudaError_t el = launch_solve(d, p, shape, grid, s->block, s->cap_stream);
+    const cudaError_t ec = cudaStreamEndCapture(s->cap_stream, &g);
+    e = el != cudaSuccess ? el : ec;
+  }
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&s->gexec, g, 0);
+  if (g) cudaGraphDestroy(g);
+  if (e != cudaSuccess) {
+    cudaGetLastError();  // not sticky: clear it and launch directly from now on
+    s->gexec = nullptr;
+    s->graph_ok = false;
+    return false;
+  }
+  std::memcpy(static_cast<void *>(&s->gd), &d, sizeof d);
+  std::memcpy(static_cast<void *>(&s->gp), &p, sizeof p);
+  s->gshape = shape; s->ggrid = grid; s->gblock = s->block;
+  *captured = true;
+  return true;
 }
 
 // One solve with launch configuration (shape, grid, dag_warps); resume keeps
@@ -762,8 +812,11 @@ static int run_solve(fim_solver *s, cudaStream_t st, int shape, int grid, int da
   d.probe = s->probe.p;
 #endif
   CUDA_TRY(s, cudaMemsetAsync(s->ctl.p, 0, sizeof(FimCtl), st));
+  bool captured = false;
+  const bool replayed = graph_prepare(s, d, p, shape, grid, &captured);
   CUDA_TRY(s, cudaEventRecord(s->ev0, st));
-  CUDA_TRY(s, launch_solve(d, p, shape, grid, s->block, st));
+  if (replayed) CUDA_TRY(s, cudaGraphLaunch(s->gexec, st));
+  else CUDA_TRY(s, launch_solve(d, p, shape, grid, s->block, st));
   CUDA_TRY(s, cudaEventRecord(s->ev1, st));
   CUDA_TRY(s, cudaMemcpyAsync(&s->last_ctl, s->ctl.p, sizeof(FimCtl), cudaMemcpyDeviceToHost, st));
   CUDA_TRY(s, cudaStreamSynchronize(st));
@@ -780,6 +833,8 @@ static int run_solve(fim_solver *s, cudaStream_t st, int shape, int grid, int da
   s->stats.batch_corners = kShapes[shape].corners;
   s->stats.dag_warps = dag_warps;
   s->stats.submesh_sweeps = p.local;
+  s->stats.graph_launch = replayed ? 1 : 0;
+  s->stats.graph_captured = captured ? 1 : 0;
 #ifdef FIM_PROBE
   print_probe(s, grid);
 #endif

@@ -47,7 +47,8 @@ class FimStats(C.Structure):
                 ("exact_evals", C.c_int64), ("solve_ms", C.c_double), ("metric_ms", C.c_double), ("n_corners", C.c_int64),
                 ("grid_blocks", C.c_int), ("block_threads", C.c_int), ("batch_slots", C.c_int),
                 ("batch_corners", C.c_int), ("dag_warps", C.c_int), ("warm_reset", C.c_int64),
-                ("warm_rounds", C.c_int), ("submesh_sweeps", C.c_int)]
+                ("warm_rounds", C.c_int), ("submesh_sweeps", C.c_int), ("graph_launch", C.c_int),
+                ("graph_captured", C.c_int)]
 
 
 class FimTuneInfo(C.Structure):

@@ -124,7 +124,12 @@ int fim_set_conduction_device(fim_solver *s, const double *d_fib, const double *
 int fim_set_stimuli(fim_solver *s, int64_t n, const int64_t *vertices, const double *t0);
 
 /* Runs the solve on `stream` (a cudaStream_t, NULL = the solver's working
- * stream) and waits for it. */
+ * stream) and waits for it.  The persistent launch is captured once into a
+ * CUDA graph (on a stream of the solver's own) and replayed by every later
+ * solve whose device buffers, stimulus count, options and launch
+ * configuration are unchanged; anything else captures a new graph.  Where
+ * capture is not available the kernel is launched directly (fim_stats
+ * graph_launch = 0). */
 int fim_solve(fim_solver *s, void *stream);
 
 /* Sets the working stream (a cudaStream_t on the solver's device) of all
@@ -153,6 +158,12 @@ typedef struct {
   int64_t warm_reset;      /* warm start: times the support check rejected  */
   int warm_rounds;         /* warm start: check-reset-resume rounds run     */
   int submesh_sweeps;      /* 1: blocks ran whole submeshes per window      */
+  int graph_launch;        /* 1: the persistent launch ran as the replay of
+                              a CUDA graph instantiated by the solver        */
+  int graph_captured;      /* 1: this solve captured (and instantiated) that
+                              graph; later solves with the same staged
+                              buffers, stimuli count and launch configuration
+                              replay it without capturing again              */
 } fim_stats;
 int fim_get_stats(const fim_solver *s, fim_stats *out);
 
