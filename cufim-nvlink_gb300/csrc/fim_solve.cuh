@@ -57,6 +57,10 @@ constexpr int kThreads = kSolveThreads;  // threads per block of the solve kerne
 #endif
 constexpr int kMarkLanes = FIM_MARK_LANES;  // threads per frozen vertex in the neighbour marking
 static_assert(kThreads % kMarkLanes == 0, "marking groups must tile the grid");
+// the two-phase path's marking (phase X): groups of kMarkLanesX threads,
+// two neighbours per thread and round
+constexpr int kMarkLanesX = 8;
+static_assert(kThreads % kMarkLanesX == 0, "marking groups must tile the block");
 constexpr int kSlots = FIM_SLOTS;             // vertices per batch (at most)
 constexpr int kCornerCap = FIM_CORNER_CAP;    // corners per batch
 constexpr int kTriCap = kCornerCap * 6 / 5;  // triangle screens per batch (more are screened on the spot)
@@ -139,7 +143,8 @@ struct BatchSh {
   float qlb[3][kQcap];              // their lower bounds (rechecked against the final bhi)
   int ntri, ntet, nedge, nq[3];
   int next_item;                    // next unclaimed screen item (phase S)
-  int nslot;                        // vertices of the current batch
+  int wsum[kSlots / 32];            // corner counts of each warp's 32 slots (setup)
+  int nfit;                         // slots whose corners end within kCornerCap (setup)
   int nfz;                          // kNarrow2: frozen slots of the batch
 };
 
@@ -428,39 +433,39 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
     }
     if (tid == 0) {
       sh.cp[0] = 0;
+      sh.nfit = 0;
       sh.ntri = 0; sh.ntet = 0; sh.nedge = 0; sh.nq[0] = 0; sh.nq[1] = 0; sh.nq[2] = 0; sh.next_item = 0; sh.nfz = 0;
     }
     __syncthreads();
-    if (tid < 32) {
-      // inclusive prefix of the corner counts (slot lane + 32 r in round r)
-      // and the longest run of slots with <= kCornerCap corners, at least one
-      int carry = 0, fit = 0;
+    // corner prefix over the slots: each warp scans its 32 slots, the warp
+    // totals are added after one barrier; then every slot marks its corners
+    // with its index (phase A reads the slot of a corner instead of
+    // searching the prefix) and the slots whose corners end within
+    // kCornerCap are counted (the batch: that run, at least one slot)
+    int cnt_own = 0, incl = 0;
+    if (tid < kSlots) {  // whole warps
+      cnt_own = tid < cand ? sh.cnt[tid] : 0;
+      incl = cnt_own;
 #pragma unroll
-      for (int r = 0; r < kSlots / 32; ++r) {
-        const int sl = tid + 32 * r;
-        int a = sl < cand ? sh.cnt[sl] : 0;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          const int u = __shfl_up_sync(FULL_MASK, a, o);
-          if (tid >= o) a += u;
-        }
-        a += carry;
-        sh.cp[sl + 1] = a;
-        fit += __popc(__ballot_sync(FULL_MASK, sl < cand && a <= kCornerCap));
-        carry = __shfl_sync(FULL_MASK, a, 31);
+      for (int o = 1; o < 32; o <<= 1) {
+        const int u = __shfl_up_sync(FULL_MASK, incl, o);
+        if (lane >= o) incl += u;
       }
-      if (tid == 0) sh.nslot = max(1, fit);
+      if (lane == 31) sh.wsum[tid >> 5] = incl;
     }
     __syncthreads();
-    const int nslot = sh.nslot;
+    if (tid < kSlots) {
+      for (int w = 0; w < (tid >> 5); ++w) incl += sh.wsum[w];
+      sh.cp[tid + 1] = incl;
+      const int fit = __popc(__ballot_sync(FULL_MASK, tid < cand && incl <= kCornerCap));
+      if (lane == 0 && fit) atomicAdd(&sh.nfit, fit);
+      const int j1 = min(incl, kCornerCap);
+      for (int j = incl - cnt_own; j < j1; ++j) sh.cs[j] = (uint8_t)tid;
+    }
+    __syncthreads();
+    const int nslot = max(1, sh.nfit);
     const int total = sh.cp[nslot];     // may exceed kCornerCap for a single huge vertex
     const int kept = min(total, kCornerCap);
-    // the slot of every corner of the batch, so that phase A issues each
-    // record load without searching the corner prefix first
-    if (tid < nslot) {
-      const int j1 = min(sh.cp[tid + 1], kept);
-      for (int j = sh.cp[tid]; j < j1; ++j) sh.cs[j] = (uint8_t)tid;
-    }
     __syncthreads();
     PROBE(kPrSetup);
 
@@ -838,20 +843,32 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
       PROBE(kPrE);
       // the downwind neighbours of the vertices frozen now (not narrow, later
       // time): stamped in their state word, first stamp wins; a group of
-      // kMarkLanes threads per frozen vertex
+      // kMarkLanesX threads per frozen vertex, two neighbours per thread and
+      // round with their loads issued together
       const int nfz = sh.nfz;
-      for (int g = tid / kMarkLanes; g < nfz; g += kThreads / kMarkLanes) {
+      for (int g = tid / kMarkLanesX; g < nfz; g += kThreads / kMarkLanesX) {
         const int slot = sh.fz[g];
         const double pn = dunkey(sh.res[slot]);
         const int64_t k0 = sh.n0[slot], k1 = k0 + sh.ncnt[slot];
-        for (int64_t k = k0 + tid % kMarkLanes; k < k1; k += kMarkLanes) {
-          const int32_t v = __ldg(d.nbr + k);
-          const uint32_t w = __ldcg(d.sw + v);
-          const double pv = __ldcg(d.phi2 + v);
-          if (sw_state(w) != ST_NARROW && sw_stamp(w) != stamp && pn < pv) {
-            if (atomicCAS(d.sw + v, w, sw_make(sw_state(w), stamp)) == w) {
-              d.tst[v] = (uint8_t)sw_state(w);
-              lo_.marked[atomicAdd(lo_.n_marked, 1)] = v;
+        for (int64_t k = k0 + tid % kMarkLanesX; k < k1; k += 2 * kMarkLanesX) {
+          const int64_t kk[2] = {k, k + kMarkLanesX};
+          int32_t v[2];
+          uint32_t w[2];
+          double pv[2];
+#pragma unroll
+          for (int h = 0; h < 2; ++h) v[h] = kk[h] < k1 ? __ldg(d.nbr + kk[h]) : -1;
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            w[h] = v[h] >= 0 ? __ldcg(d.sw + v[h]) : 0u;
+            pv[h] = v[h] >= 0 ? __ldcg(d.phi2 + v[h]) : 0.0;
+          }
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            if (v[h] >= 0 && sw_state(w[h]) != ST_NARROW && sw_stamp(w[h]) != stamp && pn < pv[h]) {
+              if (atomicCAS(d.sw + v[h], w[h], sw_make(sw_state(w[h]), stamp)) == w[h]) {
+                d.tst[v[h]] = (uint8_t)sw_state(w[h]);
+                lo_.marked[atomicAdd(lo_.n_marked, 1)] = v[h];
+              }
             }
           }
         }
