@@ -205,7 +205,7 @@ __device__ __forceinline__ CandBound tri_screen_bf(Re e12, Re e13, Re e23, Re p1
 
 // solve_tet_cu with scaled edge norms g = e13, e23, e34, e12, e14, e24 (each
 // times 2^-k), true times p1..p3 and k.
-__device__ __forceinline__ CandBound tet_screen(const Re *g, Re p1, Re p2, Re p3, int k)
+__device__ __forceinline__ CandBound tet_screen(const Re *g, Re p1, Re p2, Re p3, int k, int *why = nullptr)
 {
   CandBound r;
   r.some = CAND_SOME;
@@ -242,8 +242,8 @@ __device__ __forceinline__ CandBound tet_screen(const Re *g, Re p1, Re p2, Re p3
   const Re T6 = re_scale(ECDD - BDDD, 2.f) * E;
   const Re T7 = ((E2CC + ((B2 - re_scale(A, 2.f) * C) * D) * D) - re_scale(ECCmBCD, 2.f) * E) * F;
   const Re S = (((((((T0 + T1) - T2) + (K1 * Q13) * Q13) - (K2 * Q13) * Q23) + (K3 * Q23) * Q23) + T6) + T7);
-  if (re_hi(S) < 0.f) { r.some = CAND_NONE; return r; }  // sqt < 0: INF
-  if (!(re_lo(S) >= 0.f)) return r;                       // undecided: FP64
+  if (re_hi(S) < 0.f) { r.some = CAND_NONE; if (why) *why = 0; return r; }  // sqt < 0: INF
+  if (!(re_lo(S) >= 0.f)) { if (why) *why = 1; return r; }                 // undecided: FP64
 
   const Re PA = (((((ECDD - BDDD) + (((EC - BD) * F) * Q13) * Q13) - (re_scale(ECD - BDD, 2.f) * Q13) * Q23) +
                   (ECCmBCD * Q23) * Q23) - ECCmBCD * F);
@@ -276,7 +276,8 @@ __device__ __forceinline__ CandBound tet_screen(const Re *g, Re p1, Re p2, Re p3
     lb = fminf(lb, vl);
     if (acc && re_lo(Qs) >= 0.f) ub = fminf(ub, re_hi(V));
   }
-  if (!any) { r.some = CAND_NONE; return r; }
+  if (!any) { r.some = CAND_NONE; if (why) *why = 2; return r; }
+  if (why) *why = 3;
   r.lb = nan_lb ? NAN : lb;
   r.ub = ub;
   return r;

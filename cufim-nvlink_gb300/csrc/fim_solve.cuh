@@ -284,12 +284,12 @@ __device__ __forceinline__ CandBound tri_screen_sm(const FimDev &d, const BatchS
                     re_in(pb));
 }
 
-__device__ __forceinline__ CandBound tet_screen_sm(const FimDev &d, const BatchSh &sh, int j)
+__device__ __forceinline__ CandBound tet_screen_sm(const FimDev &d, const BatchSh &sh, int j, int *why = nullptr)
 {
   float g[7];
   screen_record(d, sh, j, g);
   const Re gs[6] = {re_in(g[0]), re_in(g[1]), re_in(g[2]), re_in(g[3]), re_in(g[4]), re_in(g[5])};
-  return tet_screen(gs, re_in(sh.pf[j][0]), re_in(sh.pf[j][1]), re_in(sh.pf[j][2]), (int)g[6]);
+  return tet_screen(gs, re_in(sh.pf[j][0]), re_in(sh.pf[j][1]), re_in(sh.pf[j][2]), (int)g[6], why);
 }
 
 // A triangle pair that finds the screen list full: screened (and solved)
@@ -669,7 +669,17 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
             slot = sh.cs[j];
             CandBound cb;
             if (exact_all) { cb.some = CAND_SOME; cb.lb = NAN; cb.ub = INFINITY; }
+#ifdef FIM_PROBE
+            else {
+              int why = 3;
+              cb = tet_screen_sm(d, sh, j, &why);
+              // outcomes: sqt < 0, sqt undecided, no accepted root, a value (pruned / queued below)
+              atomicAdd(&d.probe[blockIdx.x * kProbeSlots + 16 + (why < 3 ? why : 3)], 1ull);
+              if (why == 3 && cb.lb > funkey(sh.bhi[slot])) atomicAdd(&d.probe[blockIdx.x * kProbeSlots + 20], 1ull);
+            }
+#else
             else cb = tet_screen_sm(d, sh, j);
+#endif
             if (!exact_all && cb.some && cb.ub < INFINITY) atomicMin(&sh.bhi[slot], fkey(cb.ub));
             lb = isnan(cb.lb) ? -INFINITY : cb.lb;
             need = cb.some && !(lb > funkey(sh.bhi[slot]));
@@ -716,6 +726,10 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
               if (!exact_all && cb[h].some && cb[h].ub < INFINITY) atomicMin(&sh.bhi[sl[h]], fkey(cb[h].ub));
               lb = isnan(cb[h].lb) ? -INFINITY : cb[h].lb;
               need = cb[h].some && !(lb > funkey(sh.bhi[sl[h]]));
+#ifdef FIM_PROBE
+              // triangle outcomes: no value, a value above bhi, a value below
+              atomicAdd(&d.probe[blockIdx.x * kProbeSlots + (!cb[h].some ? 21 : (need ? 23 : 22))], 1ull);
+#endif
               if (fp32 && need && cb[h].ub < INFINITY && !isnan(cb[h].lb)) {  // FP32 mode: conclusive screen
                 atomicMin(&sh.res[sl[h]], dkey((double)(0.5f * (cb[h].lb + cb[h].ub))));
                 need = false;
@@ -743,6 +757,12 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
       // tet warps, which meet at named barrier 1 between prefix and roots
       const int tet_warps = min(dag_warps, (ntet * kDagLanes + 31) / 32);
       const int tri0 = 32 * tet_warps;
+#ifdef FIM_PROBE
+      if (tid == 0) {  // queued FP64 solves of the batch: tets (and batches with > 48), triangles
+        d.probe[blockIdx.x * kProbeSlots + 14] += (unsigned long long)ntet + ((unsigned long long)(ntet > 48) << 32);
+        d.probe[blockIdx.x * kProbeSlots + 15] += (unsigned long long)ntri + ((unsigned long long)nedge << 32);
+      }
+#endif
       if (tid < tri0) {
         const int grp = tid / kDagLanes, gl = tid % kDagLanes;
         double *S = sh.dag[grp];

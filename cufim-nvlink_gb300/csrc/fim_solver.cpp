@@ -680,8 +680,8 @@ static void print_probe(fim_solver *s, int grid)
   std::vector<unsigned long long> h((size_t)grid * kProbeSlots);
   if (cudaMemcpy(h.data(), s->probe.p, sizeof(unsigned long long) * h.size(), cudaMemcpyDeviceToHost) != cudaSuccess)
     return;
-  static const char *names[kProbeSlots] = {"setup", "A", "B", "S", "D", "E", "mark", "barrier", "light", "batches",
-                                           "phases", "S-tet warp-ms", "S-tri warp-ms", "S-edge warp-ms", "", ""};
+  static const char *names[14] = {"setup", "A", "B", "S", "D", "E", "mark", "barrier", "light", "batches",
+                                  "phases", "S-tet warp-ms", "S-tri warp-ms", "S-edge warp-ms"};
   std::fprintf(stderr, "probe (mean per block):");
   for (int k = 0; k < 14; ++k) {
     double sum = 0.0;
@@ -689,6 +689,23 @@ static void print_probe(fim_solver *s, int grid)
     sum /= grid;
     if (k < 9 || k >= 11) std::fprintf(stderr, " %s %.3f ms", names[k], sum * 1e-6);
     else std::fprintf(stderr, " %s %.1f", names[k], sum);
+  }
+  // queued FP64 solves per block: tets (low word; batches with more than 48
+  // in the high word), triangles (low) and edges (high)
+  double q[4] = {0, 0, 0, 0};
+  for (int b = 0; b < grid; ++b) {
+    const unsigned long long a = h[(size_t)b * kProbeSlots + 14], c = h[(size_t)b * kProbeSlots + 15];
+    q[0] += (double)(a & 0xffffffffull); q[1] += (double)(a >> 32);
+    q[2] += (double)(c & 0xffffffffull); q[3] += (double)(c >> 32);
+  }
+  std::fprintf(stderr, " queued tets %.1f (batches > 48: %.1f) tris %.1f edges %.1f", q[0] / grid, q[1] / grid,
+               q[2] / grid, q[3] / grid);
+  static const char *outc[8] = {"tet sqt<0", "tet sqt undecided", "tet no root", "tet value", "tet value>bhi",
+                                "tri none", "tri >bhi", "tri <=bhi"};
+  for (int k = 16; k < 24; ++k) {
+    double sum = 0.0;
+    for (int b = 0; b < grid; ++b) sum += (double)h[(size_t)b * kProbeSlots + k];
+    std::fprintf(stderr, " %s %.0f", outc[k - 16], sum / grid);
   }
   std::fprintf(stderr, "\n");
 }
