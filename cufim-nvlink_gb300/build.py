@@ -26,7 +26,7 @@ NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["fim_kernels.cu", "fim_solve_s192.cu", "fim_solve_s160.cu", "fim_solve_s96.cu", "fim_static.cu",
-              "fim_mlp.cu"]
+              "fim_mlp.cu", "fim_selftest.cu"]
 CPP_SOURCES = ["fim_solver.cpp", "fim_io.cpp", "cuda_solver_fim.cpp"]
 CLI_SOURCES = ["fim_cli.cpp"]
 

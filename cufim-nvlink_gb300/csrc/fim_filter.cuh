@@ -203,10 +203,14 @@ __device__ __forceinline__ CandBound tri_screen_bf(Re e12, Re e13, Re e23, Re p1
   return r;
 }
 
-// solve_tet_cu with scaled edge norms g = e13, e23, e34, e12, e14, e24 (each
-// times 2^-k), true times p1..p3 and k.
-__device__ __forceinline__ CandBound tet_screen(const Re *g, Re p1, Re p2, Re p3, int k, int *why = nullptr)
+// solve_tet_cu with scaled edge norms gv = e13, e23, e34, e12, e14, e24
+// (each times 2^-k, float copies), the float copies of the times p1..p3 and
+// k.
+__device__ __forceinline__ CandBound tet_screen(const float *gv, float p1f, float p2f, float p3f, int k,
+                                                int *why = nullptr)
 {
+  const Re g[6] = {re_in(gv[0]), re_in(gv[1]), re_in(gv[2]), re_in(gv[3]), re_in(gv[4]), re_in(gv[5])};
+  const Re p1 = re_in(p1f), p2 = re_in(p2f), p3 = re_in(p3f);
   CandBound r;
   r.some = CAND_SOME;
   r.lb = NAN;

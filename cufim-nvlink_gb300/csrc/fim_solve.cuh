@@ -288,8 +288,7 @@ __device__ __forceinline__ CandBound tet_screen_sm(const FimDev &d, const BatchS
 {
   float g[7];
   screen_record(d, sh, j, g);
-  const Re gs[6] = {re_in(g[0]), re_in(g[1]), re_in(g[2]), re_in(g[3]), re_in(g[4]), re_in(g[5])};
-  return tet_screen(gs, re_in(sh.pf[j][0]), re_in(sh.pf[j][1]), re_in(sh.pf[j][2]), (int)g[6], why);
+  return tet_screen(g, sh.pf[j][0], sh.pf[j][1], sh.pf[j][2], (int)g[6], why);
 }
 
 // A triangle pair that finds the screen list full: screened (and solved)

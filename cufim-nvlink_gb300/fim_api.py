@@ -30,7 +30,8 @@ EXPORTS = ["fim_default_opts", "fim_create", "fim_destroy", "fim_last_error", "f
            "fim_batch_destroy", "fim_batch_last_error", "fim_batch_add", "fim_batch_solve", "fim_batch_get_times",
            "fim_batch_get_stats", "fim_mlp_create", "fim_mlp_destroy", "fim_mlp_set_params", "fim_mlp_get_params",
            "fim_mlp_gradients", "fim_mlp_train_step", "fim_mlp_predict", "fim_features", "fim_set_warm_start",
-           "fim_autotune", "fim_get_tune", "fim_set_tune", "fim_batch_autotune", "fim_batch_set_warm_start"]
+           "fim_autotune", "fim_get_tune", "fim_set_tune", "fim_batch_autotune", "fim_batch_set_warm_start",
+           "fim_selftest_screens"]
 MLP_INPUTS = 64
 MLP_PARAMS = 41473
 
@@ -119,6 +120,7 @@ def lib():
         L.fim_set_tune.argtypes = [vp, P(FimTuneInfo)]
         L.fim_batch_autotune.argtypes = [vp, vp, P(FimTuneInfo)]
         L.fim_batch_set_warm_start.argtypes = [vp, vp]
+        L.fim_selftest_screens.argtypes = [C.c_int, i64, C.c_uint64, P(i64)]
         L.fim_vtk_read.argtypes = [C.c_char_p, P(i64), P(i64), P(d), P(i64), P(i32)]
         L.fim_vtk_write.argtypes = [C.c_char_p, i64, i64, P(d), P(i64), P(i32), P(d), P(d)]
         L.fim_read_tags.argtypes = [C.c_char_p, P(i64), P(i32)]
@@ -127,6 +129,15 @@ def lib():
             getattr(L, name)
         _lib = L
     return _lib
+
+
+def selftest_screens(n, seed=1, device=0):
+    """The FP32 screens against the FP64 solves on n random corners
+    (fim_selftest_screens): a dict of counts, violations included."""
+    out = np.zeros(6, dtype=np.int64)
+    _check(lib().fim_selftest_screens(device, n, seed, out.ctypes.data_as(C.POINTER(C.c_int64))))
+    keys = ["tets", "tet_violations", "tets_with_value", "tris", "tri_violations", "tris_with_value"]
+    return {k: int(v) for k, v in zip(keys, out)}
 
 
 def _ptr(a, t):

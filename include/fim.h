@@ -228,6 +228,17 @@ int fim_set_tune(fim_solver *s, const fim_tune_info *cfg);
 int fim_solve_noalloc(fim_solver *s, int64_t n, const int64_t *vertices, const double *t0,
                       double *d_phi, void *stream);
 
+/* Self-test of the FP32 screens -- no counterpart in the reference.  The
+ * solve screens every triangle and tet candidate with rigorous FP32 bounds
+ * before it runs the FP64 solve, and stays bit-exact only while those
+ * bounds hold.  This checks them on n random corners (random shapes and
+ * anisotropic metrics, plane-wave, spread and nearly equal times) against
+ * the FP64 solves on `device`: out[0] tets checked, out[1] tet violations,
+ * out[2] tets with a value, out[3] triangle pairs checked, out[4] triangle
+ * violations, out[5] triangle pairs with a value.  A violation is a value
+ * the screen calls impossible or bounds wrongly. */
+int fim_selftest_screens(int device, int64_t n, uint64_t seed, int64_t *out);
+
 /* Batched solves -- no counterpart in the reference: many solves of uneven
  * size in one persistent launch.
  * Independent problems (mesh + conduction + stimuli, each with its own
