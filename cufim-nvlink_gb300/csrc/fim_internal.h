@@ -103,7 +103,7 @@ struct FimDev {
 
 // Iteration stamps live in the upper 24 bits of the state word.
 constexpr int64_t kMaxStampIterations = (int64_t(1) << 24) - 1;
-constexpr int kProbeSlots = 24;  // phase-time accumulators per block (FIM_PROBE builds)
+constexpr int kProbeSlots = 28;  // phase-time accumulators per block (FIM_PROBE builds)
 
 struct FimParams {
   double dt;            // window length (inf = endless)

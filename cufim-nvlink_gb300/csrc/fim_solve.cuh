@@ -743,6 +743,11 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
     }
     __syncthreads();
     PROBE(kPrS);
+#ifdef FIM_PROBE
+    __shared__ unsigned long long s_d_start, s_d_tri_end;
+    if (tid == 0) { s_d_start = global_timer(); s_d_tri_end = 0; }
+    __syncthreads();
+#endif
 
     // D: exact solves; tets (a lane group each) from thread 0, triangles and
     // edges each from the next warp boundary
@@ -800,6 +805,12 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
           }
           asm volatile("bar.sync 1, %0;" ::"r"(tri0) : "memory");  // the next pass overwrites the scratch
         }
+#ifdef FIM_PROBE
+        if (tid == 0) {  // the tet part of D, in batches that have one
+          d.probe[blockIdx.x * kProbeSlots + 24] += global_timer() - s_d_start;
+          d.probe[blockIdx.x * kProbeSlots + 26] += 1;
+        }
+#endif
       }
       const int edge0 = tri0 + ((ntri + 31) & ~31);
       for (int j = tid; j < edge0 + nedge; j += kThreads) {  // threads past the tets' warps: concurrently
@@ -817,9 +828,18 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
         const double val = qi == 2 ? exact_edge(d, ph, c, kind, pick3(nb, kind)) : exact_tri(d, ph, c, kind, nb);
         if (val < FIM_INF) atomicMin(&sh.res[slot], dkey(val));
         if (qi < 2) ++n_exact;
+#ifdef FIM_PROBE
+        atomicMax(&s_d_tri_end, global_timer());
+#endif
       }
     }
     __syncthreads();
+#ifdef FIM_PROBE
+    if (tid == 0 && s_d_tri_end > s_d_start) {  // the triangle/edge part of D
+      d.probe[blockIdx.x * kProbeSlots + 25] += s_d_tri_end - s_d_start;
+      d.probe[blockIdx.x * kProbeSlots + 27] += 1;
+    }
+#endif
     PROBE(kPrD);
 
     // E: decisions

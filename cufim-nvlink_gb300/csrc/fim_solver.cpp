@@ -707,6 +707,12 @@ static void print_probe(fim_solver *s, int grid)
     for (int b = 0; b < grid; ++b) sum += (double)h[(size_t)b * kProbeSlots + k];
     std::fprintf(stderr, " %s %.0f", outc[k - 16], sum / grid);
   }
+  double dt[4] = {0, 0, 0, 0};
+  for (int b = 0; b < grid; ++b)
+    for (int k = 0; k < 4; ++k) dt[k] += (double)h[(size_t)b * kProbeSlots + 24 + k];
+  std::fprintf(stderr, " D tet part %.2f us in %.1f batches, D tri part %.2f us in %.1f batches",
+               dt[2] > 0 ? dt[0] / dt[2] * 1e-3 : 0.0, dt[2] / grid, dt[3] > 0 ? dt[1] / dt[3] * 1e-3 : 0.0,
+               dt[3] / grid);
   std::fprintf(stderr, "\n");
 }
 #endif

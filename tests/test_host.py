@@ -20,7 +20,7 @@ def F(built_library):
 
 def test_exports_every_declared_symbol(F):
     header = open(os.path.join(ROOT, "include", "fim.h")).read()
-    declared = set(re.findall(r"^(?:const\s+)?\w+\s*\*?\s*(fim_[a-z_]+)\s*\(", header, re.M))
+    declared = set(re.findall(r"^(?:const\s+)?\w+\s*\*?\s*(fim_[a-z0-9_]+)\s*\(", header, re.M))
     assert declared, "no declarations found"
     L = F.lib()
     for name in sorted(declared):
