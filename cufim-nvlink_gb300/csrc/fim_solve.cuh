@@ -178,6 +178,20 @@ __device__ __forceinline__ int warp_append(int *counter, bool need, int lane)
   return need ? base + __popc(mask & ((1u << lane) - 1u)) : -1;
 }
 
+// Appends v to a global list from inside a divergent branch: one atomic per
+// group of lanes that reach it together (instead of one per lane on the
+// list's single counter).
+__device__ __forceinline__ void append_active(int32_t *list, int32_t *counter, int32_t v)
+{
+  const unsigned act = __activemask();
+  const int lane = threadIdx.x & 31;
+  const int leader = __ffs(act) - 1;
+  int base = 0;
+  if (lane == leader) base = atomicAdd(counter, __popc(act));
+  base = __shfl_sync(act, base, leader);
+  list[base + __popc(act & ((1u << lane) - 1u))] = v;
+}
+
 // One FP64 local solve of corner c with neighbours nb, on the times ph:
 // kind 0..2 are the triangle solves (1,2), (2,3), (1,3) and kind 3 the tet solve.
 __device__ __forceinline__ double exact_solve(const FimDev &d, const double *ph, int64_t c, int kind,
@@ -856,7 +870,7 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
             d.sw[v] = ST_NEXT;
           } else if (fabs(old - nw) < (1e-6 * (1 + (old + nw) * .5))) {
             d.tst[v] = ST_FROZEN;
-            lo_.frozen[atomicAdd(lo_.n_frozen, 1)] = v;
+            append_active(lo_.frozen, lo_.n_frozen, v);
           }
         } else {
           lo_.dec[pos + slot] = (nw < old) ? (uint8_t)ST_NARROW : __ldcg(d.tst + v);
@@ -906,7 +920,7 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
             if (v[h] >= 0 && sw_state(w[h]) != ST_NARROW && sw_stamp(w[h]) != stamp && pn < pv[h]) {
               if (atomicCAS(d.sw + v[h], w[h], sw_make(sw_state(w[h]), stamp)) == w[h]) {
                 d.tst[v[h]] = (uint8_t)sw_state(w[h]);
-                lo_.marked[atomicAdd(lo_.n_marked, 1)] = v[h];
+                append_active(lo_.marked, lo_.n_marked, v[h]);
               }
             }
           }
@@ -1161,7 +1175,7 @@ __global__ void __launch_bounds__(kThreads, 1) fim_solve_kernel(FimDev d, FimPar
           set_phi_both(d, v, FIM_INF); d.sw[v] = ST_FAR;
         }
       }
-      if (stv == ST_NARROW) d.list[s][atomicAdd(&ctl->n_narrow[s], 1)] = (int32_t)v;
+      if (stv == ST_NARROW) append_active(d.list[s], &ctl->n_narrow[s], (int32_t)v);
     }
     if (!grid_sync_probed(d, nblocks, p.timeout_ns, ++where)) return;
 
@@ -1262,7 +1276,7 @@ __global__ void __launch_bounds__(kThreads, 1) fim_solve_kernel(FimDev d, FimPar
             if (sw_state(w) != ST_NARROW && sw_stamp(w) != stamp && pn < pv) {
               if (atomicCAS(d.sw + v, w, sw_make(ST_NEIG, stamp)) == w) {
                 d.tst[v] = (uint8_t)sw_state(w);
-                d.lmarked[atomicAdd(&ctl->n_marked[s], 1)] = v;
+                append_active(d.lmarked, &ctl->n_marked[s], v);
               }
             }
           }
@@ -1288,7 +1302,7 @@ __global__ void __launch_bounds__(kThreads, 1) fim_solve_kernel(FimDev d, FimPar
             set_phi(d, v, __ldcg(d.phi2 + v));
             if (sv == ST_NARROW) {
               if (tv == ST_FROZEN) sv = ST_FROZEN;
-              else lnext[atomicAdd(&ctl->n_narrow[s1], 1)] = v;
+              else append_active(lnext, &ctl->n_narrow[s1], v);
             }
             d.sw[v] = sw_make(sv, stamp);  // keeps the stamp: the narrow loop below skips it
           } else {
@@ -1299,7 +1313,7 @@ __global__ void __launch_bounds__(kThreads, 1) fim_solve_kernel(FimDev d, FimPar
             if (sw_stamp(w) == stamp) continue;  // re-solved above
             if (sw_state(w) == ST_NARROW) {
               if (tv == ST_FROZEN) d.sw[v] = ST_FROZEN;
-              else lnext[atomicAdd(&ctl->n_narrow[s1], 1)] = v;
+              else append_active(lnext, &ctl->n_narrow[s1], v);
             }
           }
         }
