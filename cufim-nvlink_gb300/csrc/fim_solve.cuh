@@ -128,11 +128,11 @@ struct BatchSh {
   union {
     struct {
       float pf[kCornerCap][3];      // their float times
-      float sf[kCornerCap][3];      // float edge lengths sqrt(e14), sqrt(e24), sqrt(e34); in the exact mode phase A replaces them by the edges' lower bounds
+      float lbv[kCornerCap][4];     // lower bounds of the triangle pairs (1,2), (2,3), (1,3) and the tet (+inf: not valid)
+      float elo[kCornerCap];        // smallest lower bound of the corner's valid edges (+inf: none)
     };
     double dag[kDagGroups][kDagSlots];  // phase D (where pf and sf are dead): scratch of the tet prefix groups
   };
-  uint32_t hb[kCornerCap][2];       // root-term bounds of pairs (1,2), (2,3) | (1,3), tet: fp16 pairs rounded down
   uint8_t vm[kCornerCap];           // validity bits of the three neighbours
   uint8_t cs[kCornerCap];           // slot of the corner's vertex
   // compacted screen lists: items corner j | pair k << 14 (triangles), corner j (tets)
@@ -513,31 +513,40 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
           pf[i] = __ldcg(phf + nbs[i]);
           stn[i] = (uint8_t)sw_seen(__ldcg(d.sw + nbs[i]), kMarkedMode, stamp);
         }
-        sh.hb[j][0] = h0.w;
-        sh.hb[j][1] = h1.w;
         const float len[3] = {__uint_as_float(h1.x), __uint_as_float(h1.y), __uint_as_float(h1.z)};
         uint32_t m = 0;
-        float ub = INFINITY;
+        float ub = INFINITY, elo = INFINITY, lo[3], hi[3];
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
           const Re P = re_in(pf[i]);
+          lo[i] = re_lo(P);
+          hi[i] = re_hi(P);
           bool ok = stn[i] >= ST_NARROW;
           if (ok) {
-            if (re_lo(P) > lower_hi) ok = true;
-            else if (re_hi(P) <= lower_lo) ok = false;
+            if (lo[i] > lower_hi) ok = true;
+            else if (hi[i] <= lower_lo) ok = false;
             else ok = __ldcg(ph + nbs[i]) > lower;  // rare: the FP64 time decides
           }
           if (ok) {
             m |= 1u << i;
             const Re E = P + re_len(len[i]);
             ub = fminf(ub, re_hi(E));
-            // exact mode: the edge's lower bound replaces its length
-            sh.sf[j][i] = fp32 ? len[i] : re_lo(E);
-          } else {
-            sh.sf[j][i] = fp32 ? len[i] : INFINITY;
+            elo = fminf(elo, re_lo(E));
           }
           sh.pf[j][i] = pf[i];
         }
+        // lower bounds of the triangle pairs and the tet: min(times) +
+        // root-term bound (fp16, rounded down), for phase B's screen lists
+        const float hv[4] = {half_lo(h0.w), half_hi(h0.w), half_lo(h1.w), half_hi(h1.w)};
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          const int a = k == 1 ? 1 : 0, b = k == 0 ? 1 : 2;
+          sh.lbv[j][k] = ((m >> a) & (m >> b) & 1u) ? solve_lo(fminf(lo[a], lo[b]), fmaxf(hi[a], hi[b]), hv[k])
+                                                     : INFINITY;
+        }
+        sh.lbv[j][3] = m == 7u ? solve_lo(fminf(lo[0], fminf(lo[1], lo[2])), fmaxf(hi[0], fmaxf(hi[1], hi[2])), hv[3])
+                               : INFINITY;
+        sh.elo[j] = elo;
         if (m) ++n_filtered;
         if (!exact_all && ub < INFINITY) atomicMin(&sh.bhi[slot], fkey(ub));
         sh.vm[j] = (uint8_t)m;
@@ -555,24 +564,13 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
       const bool in = j < kept;
       int slot = 0;
       uint32_t m = 0;
-      float bhi = 0.f, lb[4] = {0.f, 0.f, 0.f, 0.f};
+      float bhi = 0.f, lb[4] = {0.f, 0.f, 0.f, 0.f}, elo = 0.f;
       if (in) {
         slot = sh.cs[j];
         m = sh.vm[j];
         bhi = funkey(sh.bhi[slot]);
-        // lower bounds of the triangle pairs and the tet: min(times) + root-term bound
-        float lo[3], hi[3];
-#pragma unroll
-        for (int i = 0; i < 3; ++i) {
-          const Re P = re_in(sh.pf[j][i]);
-          lo[i] = re_lo(P);
-          hi[i] = re_hi(P);
-        }
-        const uint32_t w0 = sh.hb[j][0], w1 = sh.hb[j][1];
-        lb[0] = solve_lo(fminf(lo[0], lo[1]), fmaxf(hi[0], hi[1]), half_lo(w0));
-        lb[1] = solve_lo(fminf(lo[1], lo[2]), fmaxf(hi[1], hi[2]), half_hi(w0));
-        lb[2] = solve_lo(fminf(lo[0], lo[2]), fmaxf(hi[0], hi[2]), half_lo(w1));
-        lb[3] = solve_lo(fminf(lo[0], fminf(lo[1], lo[2])), fmaxf(hi[0], fmaxf(hi[1], hi[2])), half_hi(w1));
+        lb[0] = sh.lbv[j][0]; lb[1] = sh.lbv[j][1]; lb[2] = sh.lbv[j][2]; lb[3] = sh.lbv[j][3];
+        elo = sh.elo[j];
       }
       // triangle pairs (1,2), (2,3), (1,3), appended together (one atomic
       // per warp for the three), then the tet
@@ -612,7 +610,7 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
         // smallest edge lower bound (phase A) against bhi; the FP32 mode
         // lists every corner with a valid edge
         bool need = false;
-        if (in) need = fp32 ? m != 0u : !(fminf(sh.sf[j][0], fminf(sh.sf[j][1], sh.sf[j][2])) > bhi);
+        if (in) need = fp32 ? m != 0u : !(elo > bhi);
         const int p = warp_append(&sh.nedge, need, lane);
         if (p >= 0) sh.edg[p] = (uint16_t)j;  // one entry per corner at most: never full
       }
@@ -649,21 +647,25 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
 #endif
         if (cl >= edge_c0) {
           // the edges that can still be the minimum, over the corners phase
-          // B listed (sf holds the edges' lower bounds, or their lengths in
-          // the FP32 mode)
+          // B listed (their float lengths from the first-read record again)
           const int e = cl - edge_c0 + lane;
           const bool in = e < nedge;
           const int j = in ? (int)sh.edg[e] : 0;
           int slot = 0;
           uint32_t m = 0;
           float bhi = 0.f;
-          if (in) { slot = sh.cs[j]; m = sh.vm[j]; bhi = funkey(sh.bhi[slot]); }
+          uint4 r1 = make_uint4(0u, 0u, 0u, 0u);
+          if (in) {
+            slot = sh.cs[j]; m = sh.vm[j]; bhi = funkey(sh.bhi[slot]);
+            r1 = __ldg(d.crec + kCrecWords * (sh.c0[slot] + (j - sh.cp[slot])) + 1);
+          }
+          const float len[3] = {__uint_as_float(r1.x), __uint_as_float(r1.y), __uint_as_float(r1.z)};
 #pragma unroll
           for (int i = 0; i < 3; ++i) {
-            const float le = !in ? 0.f : (fp32 ? re_lo(re_in(sh.pf[j][i]) + re_len(sh.sf[j][i])) : sh.sf[j][i]);
+            const float le = in ? re_lo(re_in(sh.pf[j][i]) + re_len(len[i])) : 0.f;
             bool need = in && ((m >> i) & 1u) && !(le > bhi);
             if (fp32 && need) {  // FP32 mode: the float edge sum is the value
-              atomicMin(&sh.res[slot], dkey((double)(sh.pf[j][i] + sh.sf[j][i])));
+              atomicMin(&sh.res[slot], dkey((double)(sh.pf[j][i] + len[i])));
               need = false;
             }
             queue_exact(d, ph, sh, need, 2, i, slot, j, le, lane);
