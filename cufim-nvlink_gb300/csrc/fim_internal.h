@@ -132,9 +132,15 @@ void set_last_error(const char *msg);
 // FP64 metric + edge norms of tets [e0, e1) scattered into the corner
 // records; the first tet with a non-positive or non-finite speed or a
 // non-finite fibre lowers *bad to its index.
-cudaError_t launch_metric(const int32_t *tslots, const int64_t *cidx, const double *xyz,
-                          const double *fib, const double *cf, const double *ct, int64_t e0, int64_t e1,
+// evec: the mesh's edge vectors (launch_edge_vectors), or null to form them
+// from xyz.
+cudaError_t launch_metric(const int32_t *tslots, const int64_t *cidx, const double *xyz, const double *evec,
+                          int64_t nT, const double *fib, const double *cf, const double *ct, int64_t e0, int64_t e1,
                           double *cgeo, float *cgf, uint4 *crec, unsigned long long *bad, cudaStream_t stream);
+// Stages the six edge vectors of every tet (18 doubles, SoA) for the
+// metric kernel.
+cudaError_t launch_edge_vectors(const int32_t *tslots, const double *xyz, int64_t nT, double *evec,
+                                cudaStream_t stream);
 // The persistent cooperative solve is compiled once per batch shape
 // (fim_solve_s*.cu: vertices x corners a block stages per batch); the
 // autotuner picks the shape, the grid and the tet-prefix warps per problem.

@@ -32,7 +32,8 @@ namespace fimgb {
 // metric kernel
 
 __global__ void fim_metric_kernel(const int32_t *__restrict__ tslots, const int64_t *__restrict__ cidx,
-                                  const double *__restrict__ xyz, const double *__restrict__ fib,
+                                  const double *__restrict__ xyz, const double *__restrict__ evec, int64_t nT,
+                                  const double *__restrict__ fib,
                                   const double *__restrict__ cf, const double *__restrict__ ct,
                                   int64_t e0, int64_t e1, double *__restrict__ cgeo, float *__restrict__ cgf,
                                   uint4 *__restrict__ crec, unsigned long long *__restrict__ bad)
@@ -78,18 +79,27 @@ __global__ void fim_metric_kernel(const int32_t *__restrict__ tslots, const int6
     const double M3 = vf*fd + vs*(1. - fd);
     const double M4 = (vf - vs)*fe;
     const double M5 = vf*ff + vs*(1. - ff);
-    const int32_t v0 = tslots[4 * e + 0], v1 = tslots[4 * e + 1];
-    const int32_t v2 = tslots[4 * e + 2], v3 = tslots[4 * e + 3];
-    const int32_t va[6] = {v0, v0, v1, v0, v1, v2};
-    const int32_t vb[6] = {v1, v2, v2, v3, v3, v3};
     double g[6];
+    if (evec) {
+      // the edge vectors of the mesh, staged once (edge_vector_kernel)
 #pragma unroll
-    for (int k = 0; k < 6; ++k) {
-      // load_edge(a, b) = x_a - x_b (types.h:210-216); aMb_sym (types.h:165-171)
-      const double ex = xyz[3 * (int64_t)va[k] + 0] - xyz[3 * (int64_t)vb[k] + 0];
-      const double ey = xyz[3 * (int64_t)va[k] + 1] - xyz[3 * (int64_t)vb[k] + 1];
-      const double ez = xyz[3 * (int64_t)va[k] + 2] - xyz[3 * (int64_t)vb[k] + 2];
-      g[k] = (M0*ex + M1*ey + M2*ez)*ex + (M1*ex + M3*ey + M4*ez)*ey + (M2*ex + M4*ey + M5*ez)*ez;
+      for (int k = 0; k < 6; ++k) {
+        const double ex = evec[(3 * k + 0) * nT + e], ey = evec[(3 * k + 1) * nT + e], ez = evec[(3 * k + 2) * nT + e];
+        g[k] = (M0*ex + M1*ey + M2*ez)*ex + (M1*ex + M3*ey + M4*ez)*ey + (M2*ex + M4*ey + M5*ez)*ez;
+      }
+    } else {
+      const int32_t v0 = tslots[4 * e + 0], v1 = tslots[4 * e + 1];
+      const int32_t v2 = tslots[4 * e + 2], v3 = tslots[4 * e + 3];
+      const int32_t va[6] = {v0, v0, v1, v0, v1, v2};
+      const int32_t vb[6] = {v1, v2, v2, v3, v3, v3};
+#pragma unroll
+      for (int k = 0; k < 6; ++k) {
+        // load_edge(a, b) = x_a - x_b (types.h:210-216); aMb_sym (types.h:165-171)
+        const double ex = xyz[3 * (int64_t)va[k] + 0] - xyz[3 * (int64_t)vb[k] + 0];
+        const double ey = xyz[3 * (int64_t)va[k] + 1] - xyz[3 * (int64_t)vb[k] + 1];
+        const double ez = xyz[3 * (int64_t)va[k] + 2] - xyz[3 * (int64_t)vb[k] + 2];
+        g[k] = (M0*ex + M1*ey + M2*ez)*ex + (M1*ex + M3*ey + M4*ez)*ey + (M2*ex + M4*ey + M5*ez)*ez;
+      }
     }
     // scale 2^-k (k even) of the float screen record: edge norms O(1).  The
     // largest norm by its bit pattern (the order of non-negative doubles;
@@ -140,19 +150,47 @@ __global__ void fim_metric_kernel(const int32_t *__restrict__ tslots, const int6
   }
 }
 
+// Edge vectors of every tet in the metric kernel's edge order, x_a - x_b
+// for (a, b) = (0,1) (0,2) (1,2) (0,3) (1,3) (2,3) of its slots
+// (load_edge, types.h:210-216): they depend on the mesh only, so
+// fim_set_mesh stages them once and every conduction upload saves their 18
+// FP64 subtractions per tet.  Layout: evec[(3 k + axis) nT + e].
+__global__ void edge_vector_kernel(const int32_t *__restrict__ tslots, const double *__restrict__ xyz, int64_t nT,
+                                   double *__restrict__ evec)
+{
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nT; e += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t v0 = tslots[4 * e + 0], v1 = tslots[4 * e + 1];
+    const int32_t v2 = tslots[4 * e + 2], v3 = tslots[4 * e + 3];
+    const int32_t va[6] = {v0, v0, v1, v0, v1, v2};
+    const int32_t vb[6] = {v1, v2, v2, v3, v3, v3};
+#pragma unroll
+    for (int k = 0; k < 6; ++k)
+#pragma unroll
+      for (int a = 0; a < 3; ++a) evec[(3 * k + a) * nT + e] = xyz[3 * (int64_t)va[k] + a] - xyz[3 * (int64_t)vb[k] + a];
+  }
+}
+
 // ---------------------------------------------------------------------------
 // launch wrappers
 
-cudaError_t launch_metric(const int32_t *tslots, const int64_t *cidx, const double *xyz,
-                          const double *fib, const double *cf, const double *ct, int64_t e0, int64_t e1,
+cudaError_t launch_edge_vectors(const int32_t *tslots, const double *xyz, int64_t nT, double *evec,
+                                cudaStream_t stream)
+{
+  if (nT <= 0) return cudaSuccess;
+  edge_vector_kernel<<<152 * 8, 256, 0, stream>>>(tslots, xyz, nT, evec);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_metric(const int32_t *tslots, const int64_t *cidx, const double *xyz, const double *evec,
+                          int64_t nT, const double *fib, const double *cf, const double *ct, int64_t e0, int64_t e1,
                           double *cgeo, float *cgf, uint4 *crec, unsigned long long *bad, cudaStream_t stream)
 {
   if (e1 <= e0) return cudaSuccess;
   const int block = 256;
   int64_t grid = (e1 - e0 + block - 1) / block;
   if (grid > 152 * 64) grid = 152 * 64;
-  fim_metric_kernel<<<(unsigned)grid, block, 0, stream>>>(tslots, cidx, xyz, fib, cf, ct, e0, e1, cgeo, cgf, crec,
-                                                          bad);
+  fim_metric_kernel<<<(unsigned)grid, block, 0, stream>>>(tslots, cidx, xyz, evec, nT, fib, cf, ct, e0, e1, cgeo, cgf,
+                                                          crec, bad);
   return cudaGetLastError();
 }
 

@@ -120,6 +120,7 @@ struct fim_solver {
   double front_width = 0.0;
   DevBuf<double> xyz;
   DevBuf<int32_t> tslots;
+  DevBuf<double> evec;  // edge vectors of every tet (metric kernel); empty when they did not fit
   DevBuf<int64_t> cidx, cptr, nptr;
   DevBuf<uint4> crec;
   DevBuf<double> cgeo;
@@ -517,6 +518,14 @@ extern "C" int fim_set_mesh(fim_solver *s, int64_t nV, const double *xyz, int64_
   cudaStream_t st = s->stream;
   CUDA_TRY(s, cudaMemcpyAsync(s->xyz.p, xyz, sizeof(double) * 3 * nV, cudaMemcpyHostToDevice, st));
   CUDA_TRY(s, cudaMemcpyAsync(s->tslots.p, slots.data(), sizeof(int32_t) * 4 * nT, cudaMemcpyHostToDevice, st));
+  // the edge vectors for the metric kernel (144 B per tet); without room
+  // for them the kernel forms them from xyz
+  if (s->evec.alloc((size_t)18 * nT) == cudaSuccess) {
+    CUDA_TRY(s, launch_edge_vectors(s->tslots.p, s->xyz.p, nT, s->evec.p, st));
+  } else {
+    cudaGetLastError();
+    s->evec.release();
+  }
   CUDA_TRY(s, cudaMemcpyAsync(s->cidx.p, cidx.data(), sizeof(int64_t) * nC, cudaMemcpyHostToDevice, st));
   CUDA_TRY(s, cudaMemcpyAsync(s->cptr.p, cptr.data(), sizeof(int64_t) * (nL + 1), cudaMemcpyHostToDevice, st));
   CUDA_TRY(s, cudaStreamSynchronize(st));
@@ -572,8 +581,8 @@ static int run_metric(fim_solver *s, const double *fib, const double *cf, const 
     CUDA_TRY(s, cudaEventRecord(s->ev_chunk[i], cs));
     CUDA_TRY(s, cudaStreamWaitEvent(s->stream, s->ev_chunk[i], 0));
     if (i == 0) CUDA_TRY(s, cudaEventRecord(s->ev0, s->stream));
-    CUDA_TRY(s, launch_metric(s->tslots.p, s->cidx.p, s->xyz.p, s->fib.p, s->cf.p, s->ct.p, e0, e1, s->cgeo.p,
-                              s->cgf.p, s->crec.p, s->bad.p, s->stream));
+    CUDA_TRY(s, launch_metric(s->tslots.p, s->cidx.p, s->xyz.p, s->evec.p, s->nT, s->fib.p, s->cf.p, s->ct.p, e0,
+                              e1, s->cgeo.p, s->cgf.p, s->crec.p, s->bad.p, s->stream));
   }
   CUDA_TRY(s, cudaEventRecord(s->ev1, s->stream));
   CUDA_TRY(s, cudaEventSynchronize(s->ev1));
