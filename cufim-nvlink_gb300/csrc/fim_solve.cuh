@@ -80,8 +80,12 @@ constexpr int kDagGroups = kDagWarps * 32 / kDagLanes;
 // needs only two: kNarrow2 updates the narrow list and marks the downwind
 // neighbours of the vertices it freezes, kMarked2 re-solves them, applies
 // everything and builds the next list.
-enum : int { kNarrow4 = 0, kMarked4 = 1, kNarrow2 = 2, kMarked2 = 3 };
-__host__ __device__ constexpr bool is_marked_mode(int m) { return m == kMarked4 || m == kMarked2; }
+// With windows the re-solve applies its own results too (kMarked3: the
+// times into both buffers, the decided state, the next list), so that
+// iteration needs three phases: a re-solved vertex is seen as "neig" by every
+// other re-solve of the phase, so nothing reads what it writes.
+enum : int { kNarrow4 = 0, kMarked4 = 1, kNarrow2 = 2, kMarked2 = 3, kMarked3 = 4 };
+__host__ __device__ constexpr bool is_marked_mode(int m) { return m == kMarked4 || m == kMarked2 || m == kMarked3; }
 
 // Order-preserving map of floats to unsigned integers (for atomicMin).
 __device__ __forceinline__ unsigned int fkey(float x)
@@ -122,7 +126,7 @@ struct BatchSh {
   unsigned int bhi[kSlots];         // fkey of a float upper bound of the new time
   int64_t n0[kSlots];               // kNarrow2: neighbourhood range of each vertex (marking)
   int32_t ncnt[kSlots];
-  uint8_t tsv[kSlots];              // kMarked2: tmp_state of each vertex
+  uint8_t tsv[kSlots];              // kMarked2, kMarked3: tmp_state of each vertex
   int32_t fz[kSlots];               // kNarrow2: slots frozen in this batch
   // per corner of the batch
   union {
@@ -442,7 +446,7 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
         sh.n0[tid] = a;
         sh.ncnt[tid] = (int32_t)(d.nptr[v + 1] - a);
       }
-      if (MODE == kMarked2) sh.tsv[tid] = __ldcg(d.tst + v);
+      if (MODE == kMarked2 || MODE == kMarked3) sh.tsv[tid] = __ldcg(d.tst + v);
     }
     if (tid == 0) {
       sh.cp[0] = 0;
@@ -928,7 +932,7 @@ __device__ void update_phase(const FimDev &d, BatchSh &sh, const int32_t *list, 
           }
         }
       }
-    } else {  // kMarked2
+    } else {  // kMarked2, kMarked3
       if (tid < kSlots) {  // whole warps: the next-list appends are warp-aggregated
         const int slot = tid;
         const bool in = slot < nslot;
@@ -1285,40 +1289,26 @@ __global__ void __launch_bounds__(kThreads, 1) fim_solve_kernel(FimDev d, FimPar
         }
         if (!grid_sync_probed(d, nblocks, p.timeout_ns, ++where)) return;
 
-        // P3 -- solve elements for neighbours + reduce (cuda_fim.cu:2215-2289)
-        const int32_t nm = ld_volatile_i32(&ctl->n_marked[s]);
-        update_phase<kMarked4>(d, sh, d.lmarked, nm, lower, lower_lo, lower_hi, phi_start, p.dt, p.exact_all != 0, p.fp32 != 0,
-                               stamp, dag, lo, my_evals, my_exact);
-        my_updates += (gtid == 0) ? nm : 0;
-        if (!grid_sync_probed(d, nblocks, p.timeout_ns, ++where)) return;
-
-        // P4 -- apply, update neighbour states, next narrow list (cuda_fim.cu:2291-2317):
-        // the re-solved neighbours, then (one index space, so that both run
-        // at once: they touch disjoint vertices) the narrow vertices that
-        // were not re-solved
-        for (int64_t i = gtid; i < (int64_t)nm + nn; i += nthreads) {
-          if (i < nm) {
-            const int32_t v = d.lmarked[i];
-            uint8_t sv = __ldcg(d.dec + i);
-            const uint8_t tv = __ldcg(d.tst + v);
-            set_phi(d, v, __ldcg(d.phi2 + v));
-            if (sv == ST_NARROW) {
-              if (tv == ST_FROZEN) sv = ST_FROZEN;
-              else append_active(lnext, &ctl->n_narrow[s1], v);
-            }
-            d.sw[v] = sw_make(sv, stamp);  // keeps the stamp: the narrow loop below skips it
-          } else {
-            // the three loads at once (a re-solved vertex's are not used)
-            const int32_t v = lst[i - nm];
-            const uint32_t w = __ldcg(d.sw + v);
-            const uint8_t tv = __ldcg(d.tst + v);
-            if (sw_stamp(w) == stamp) continue;  // re-solved above
-            if (sw_state(w) == ST_NARROW) {
-              if (tv == ST_FROZEN) d.sw[v] = ST_FROZEN;
-              else append_active(lnext, &ctl->n_narrow[s1], v);
-            }
+        // P3 -- the narrow vertices that are not re-solved now go to the next
+        // list (or freeze), then the marked neighbours are re-solved
+        // (cuda_fim.cu:2215-2289), each applying its own result, decided
+        // state and next-list entry (cuda_fim.cu:2291-2317): the two touch
+        // disjoint vertices, and a narrow vertex's state change leaves it a
+        // valid neighbour
+        for (int64_t i = gtid; i < nn; i += nthreads) {
+          const int32_t v = lst[i];
+          const uint32_t w = __ldcg(d.sw + v);
+          const uint8_t tv = __ldcg(d.tst + v);
+          if (sw_stamp(w) == stamp) continue;  // re-solved below
+          if (sw_state(w) == ST_NARROW) {
+            if (tv == ST_FROZEN) d.sw[v] = ST_FROZEN;
+            else append_active(lnext, &ctl->n_narrow[s1], v);
           }
         }
+        const int32_t nm = ld_volatile_i32(&ctl->n_marked[s]);
+        update_phase<kMarked3>(d, sh, d.lmarked, nm, lower, lower_lo, lower_hi, phi_start, p.dt, p.exact_all != 0, p.fp32 != 0,
+                               stamp, dag, lo, my_evals, my_exact);
+        my_updates += (gtid == 0) ? nm : 0;
         ++it;
         ++it_window;
         if (!grid_sync_probed(d, nblocks, p.timeout_ns, ++where)) return;
