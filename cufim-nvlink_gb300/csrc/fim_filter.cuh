@@ -205,9 +205,10 @@ __device__ __forceinline__ CandBound tri_screen_bf(Re e12, Re e13, Re e23, Re p1
 
 // solve_tet_cu with scaled edge norms gv = e13, e23, e34, e12, e14, e24
 // (each times 2^-k, float copies), the float copies of the times p1..p3 and
-// k.
-__device__ __forceinline__ CandBound tet_screen(const float *gv, float p1f, float p2f, float p3f, int k,
-                                                int *why = nullptr)
+// k.  kBf: the two roots as independent branch-free chains (re_div_bf,
+// re_sqrt_bf; the same decisions), so that they interleave.
+template <bool kBf>
+__device__ __forceinline__ CandBound tet_screen_t(const float *gv, float p1f, float p2f, float p3f, int k, int *why)
 {
   const Re g[6] = {re_in(gv[0]), re_in(gv[1]), re_in(gv[2]), re_in(gv[3]), re_in(gv[4]), re_in(gv[5])};
   const Re p1 = re_in(p1f), p2 = re_in(p2f), p3 = re_in(p3f);
@@ -261,30 +262,60 @@ __device__ __forceinline__ CandBound tet_screen(const float *gv, float p1f, floa
 
   float lb = INFINITY, ub = INFINITY;
   bool any = false, nan_lb = false;
+  if constexpr (kBf) {
 #pragma unroll
-  for (int root = 0; root < 2; ++root) {
-    const Re L2 = re_div(root == 0 ? PA + SX : PA - SX, PB);
-    if (re_hi(L2) <= 0.f || re_lo(L2) >= 1.f) continue;
-    const Re L1 = re_div(-((F * L2 + E) * Q13 - (D * L2 + B) * Q23), X);
-    if (re_hi(L1) <= 0.f || re_lo(L1) >= 1.f) continue;
-    const Re L3 = (ONE - L1) - L2;
-    if (re_hi(L3) <= 0.f) continue;
-    const bool acc = re_lo(L1) > 0.f && re_hi(L1) < 1.f && re_lo(L2) > 0.f && re_hi(L2) < 1.f && re_lo(L3) > 0.f;
-    const Re L1x2 = re_scale(L1, 2.f);
-    const Re Qs = ((((A + L1x2 * B) + (L1 * L1) * C) + (L1x2 * L2) * D) + re_scale(L2, 2.f) * E) + (L2 * L2) * F;
-    if (re_hi(Qs) < 0.f) continue;  // NaN value, dropped by fmin
-    const Re V = ((L1 * p1 + L2 * p2) + L3 * p3) + re_scale(re_sqrt(Qs), sk);
-    any = true;
-    const float vl = re_lo(V);
-    if (isnan(vl)) nan_lb = true;
-    lb = fminf(lb, vl);
-    if (acc && re_lo(Qs) >= 0.f) ub = fminf(ub, re_hi(V));
+    for (int root = 0; root < 2; ++root) {
+      const Re L2 = re_div_bf(root == 0 ? PA + SX : PA - SX, PB);
+      const Re L1 = re_div_bf(-((F * L2 + E) * Q13 - (D * L2 + B) * Q23), X);
+      const Re L3 = (ONE - L1) - L2;
+      const Re L1x2 = re_scale(L1, 2.f);
+      const Re Qs = ((((A + L1x2 * B) + (L1 * L1) * C) + (L1x2 * L2) * D) + re_scale(L2, 2.f) * E) + (L2 * L2) * F;
+      const Re V = ((L1 * p1 + L2 * p2) + L3 * p3) + re_scale(re_sqrt_bf(Qs), sk);
+      const bool use = !(re_hi(L2) <= 0.f || re_lo(L2) >= 1.f) && !(re_hi(L1) <= 0.f || re_lo(L1) >= 1.f) &&
+                       !(re_hi(L3) <= 0.f) && !(re_hi(Qs) < 0.f);
+      const bool acc = re_lo(L1) > 0.f && re_hi(L1) < 1.f && re_lo(L2) > 0.f && re_hi(L2) < 1.f && re_lo(L3) > 0.f;
+      const float vl = re_lo(V);
+      any = any || use;
+      nan_lb = nan_lb || (use && isnan(vl));
+      lb = use ? fminf(lb, vl) : lb;
+      ub = (use && acc && re_lo(Qs) >= 0.f) ? fminf(ub, re_hi(V)) : ub;
+    }
+  } else {
+#pragma unroll
+    for (int root = 0; root < 2; ++root) {
+      const Re L2 = re_div(root == 0 ? PA + SX : PA - SX, PB);
+      if (re_hi(L2) <= 0.f || re_lo(L2) >= 1.f) continue;
+      const Re L1 = re_div(-((F * L2 + E) * Q13 - (D * L2 + B) * Q23), X);
+      if (re_hi(L1) <= 0.f || re_lo(L1) >= 1.f) continue;
+      const Re L3 = (ONE - L1) - L2;
+      if (re_hi(L3) <= 0.f) continue;
+      const bool acc = re_lo(L1) > 0.f && re_hi(L1) < 1.f && re_lo(L2) > 0.f && re_hi(L2) < 1.f && re_lo(L3) > 0.f;
+      const Re L1x2 = re_scale(L1, 2.f);
+      const Re Qs = ((((A + L1x2 * B) + (L1 * L1) * C) + (L1x2 * L2) * D) + re_scale(L2, 2.f) * E) + (L2 * L2) * F;
+      if (re_hi(Qs) < 0.f) continue;  // NaN value, dropped by fmin
+      const Re V = ((L1 * p1 + L2 * p2) + L3 * p3) + re_scale(re_sqrt(Qs), sk);
+      any = true;
+      const float vl = re_lo(V);
+      if (isnan(vl)) nan_lb = true;
+      lb = fminf(lb, vl);
+      if (acc && re_lo(Qs) >= 0.f) ub = fminf(ub, re_hi(V));
+    }
   }
   if (!any) { r.some = CAND_NONE; if (why) *why = 2; return r; }
   if (why) *why = 3;
   r.lb = nan_lb ? NAN : lb;
   r.ub = ub;
   return r;
+}
+__device__ __forceinline__ CandBound tet_screen(const float *gv, float p1f, float p2f, float p3f, int k,
+                                                int *why = nullptr)
+{
+  return tet_screen_t<false>(gv, p1f, p2f, p3f, k, why);
+}
+__device__ __forceinline__ CandBound tet_screen_bf(const float *gv, float p1f, float p2f, float p3f, int k,
+                                                   int *why = nullptr)
+{
+  return tet_screen_t<true>(gv, p1f, p2f, p3f, k, why);
 }
 
 // Per-corner lower bounds, in true units, of the square-root term of the

@@ -11,7 +11,8 @@
 // random spread, nearly equal times), offset by up to 100.  The screens get
 // what the solve gives them: the squared edge norms scaled by 2^-k (k even,
 // the largest in [0.5, 4)) as floats and the float copies of the times.
-// Violations: a solve with a value that the screen calls impossible or puts
+// Both tet screens are checked (with branches, and the branch-free one the
+// solve uses).  Violations: a solve with a value that a screen calls impossible or puts
 // outside [lb, ub], or a certain upper bound where the solve has no value.
 //
 // No counterpart in the reference.
@@ -99,15 +100,15 @@ __global__ void screen_selftest_kernel(int64_t n, uint64_t seed, unsigned long l
     // tet
     {
       const double v = tet_ref(g[0], g[1], g[2], g[3], g[4], g[5], p[0], p[1], p[2]);
-      const CandBound cb = tet_screen(gs, pf[0], pf[1], pf[2], ks);
       const bool has = v < FIM_INF;  // a value (not INF, not NaN)
       bool bad = false;
-      if (has) {
-        bad = cb.some == CAND_NONE || (!isnan(cb.lb) && cb.lb > v) || cb.ub < v;
-        ++cnt[2];
-      } else {
-        bad = cb.ub < INFINITY;
+#pragma unroll
+      for (int bf = 0; bf < 2; ++bf) {  // both variants: with branches, and the solve's branch-free one
+        const CandBound cb = bf ? tet_screen_bf(gs, pf[0], pf[1], pf[2], ks) : tet_screen(gs, pf[0], pf[1], pf[2], ks);
+        if (has) bad = bad || cb.some == CAND_NONE || (!isnan(cb.lb) && cb.lb > v) || cb.ub < v;
+        else bad = bad || cb.ub < INFINITY;
       }
+      if (has) ++cnt[2];
       ++cnt[0];
       if (bad) ++cnt[1];
     }

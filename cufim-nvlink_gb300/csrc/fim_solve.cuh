@@ -276,7 +276,8 @@ __device__ __forceinline__ void queue_exact(const FimDev &d, const double *ph, B
 }
 
 // FP32 screen record of batch corner j: e13, e23, e34, e12, e14, e24 times
-// 2^-k and k (phase A has just read the record, so this hits the caches).
+// 2^-k and k (an array of its own, read only by the corners phase B lists;
+// an L1 prefetch of it issued in phase B measured slower).
 __device__ __forceinline__ void screen_record(const FimDev &d, const BatchSh &sh, int j, float *g)
 {
   const int slot = sh.cs[j];
@@ -306,7 +307,7 @@ __device__ __forceinline__ CandBound tet_screen_sm(const FimDev &d, const BatchS
 {
   float g[7];
   screen_record(d, sh, j, g);
-  return tet_screen(g, sh.pf[j][0], sh.pf[j][1], sh.pf[j][2], (int)g[6], why);
+  return tet_screen_bf(g, sh.pf[j][0], sh.pf[j][1], sh.pf[j][2], (int)g[6], why);
 }
 
 // A triangle pair that finds the screen list full: screened (and solved)
