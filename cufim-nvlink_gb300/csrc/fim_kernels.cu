@@ -14,14 +14,18 @@
 //    types.cpp:227-257), written straight into the four corner records of
 //    the tet in the relabelled order the local solver reads
 //    (gray-code tables, cuda_fim.h:41-48), plus the three edge lengths.
-//  * fim_solve_kernel -- one persistent cooperative launch for the whole
-//    solve: reset + seeding (reset_states_gpu / update_events_gpu,
-//    cuda_fim.cu:479-542, 632-683), per window update_states
-//    (cuda_fim.cu:1790-1845), then FIM iterations with the phases of
-//    compute_step (cuda_fim.cu:1992-2334) as global Jacobi steps over
-//    compacted lists (narrow list, vertices frozen this iteration,
-//    neighbours to re-solve), separated by a bounded grid barrier: four
-//    phases per iteration with windows, two with one endless window.
+//  * edge_vector_kernel -- the six edge vectors of every tet, staged once
+//    per mesh for the metric kernel;
+//  * the support check and warm-start reset of a warm-started solve.
+// The solve itself, fim_solve_kernel (fim_solve.cuh, compiled once per
+// batch shape by fim_solve_s*.cu), is one persistent cooperative launch for
+// the whole solve: reset + seeding (reset_states_gpu / update_events_gpu,
+// cuda_fim.cu:479-542, 632-683), per window update_states
+// (cuda_fim.cu:1790-1845), then FIM iterations with the phases of
+// compute_step (cuda_fim.cu:1992-2334) as global Jacobi steps over
+// compacted lists (narrow list, vertices frozen this iteration, neighbours
+// to re-solve), separated by a bounded grid barrier: three phases per
+// iteration with windows, two with one endless window.
 #include "fim_device.cuh"
 
 #include <cmath>

@@ -31,7 +31,7 @@ LEAVES = ["e13", "e23", "e34", "e12", "e14", "e24", "p1", "p2", "p3", "c0.5", "c
 NLEAF = 16
 ONE, NEGZERO = LEAVES.index("c1.0"), LEAVES.index("c-0.0")
 
-# the prefix of solve_tet_cu as written in tet_ref_root (fim_kernels.cu)
+# the prefix of solve_tet_cu as written in tet_ref (fim_device.cuh)
 EXPRS = [
     ("a", "e13"),
     ("b", "0.5 * (e23 + e13 - e12)"),
