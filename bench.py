@@ -38,8 +38,8 @@ import numpy as np  # noqa: E402
 SLAB_CELLS = (266, 93, 40)
 # DRAM bytes (read + write) of one fim_solve_kernel launch per vertex update,
 # from ncu dram__bytes_read.sum + dram__bytes_write.sum on this workload
-# (ncu measurement: 4.274 GB for 4,689,493 vertex updates, two-phase kernel, 192x4096 batches)
-NCU_DRAM_BYTES_PER_VERTEX_UPDATE = 4.274e9 / 4689493
+# (ncu measurement: 4.294 GB for 4,689,493 vertex updates, two-phase kernel, 192x4096 batches)
+NCU_DRAM_BYTES_PER_VERTEX_UPDATE = 4.294e9 / 4689493
 
 
 def metric_launches(nT):
