@@ -249,7 +249,8 @@ def parity_report(phi, phi_o, tolerance="max |dt| <= 1e-4 max(t); achieved bit-e
     same_inf = bool(np.array_equal(phi >= 1e300, ~finite))
     return {"max_abs_err": float(d.max()), "max_rel_err": float(d.max() / tmax),
             "rms_rel_err": float(np.sqrt(np.mean(d ** 2)) / tmax),
-            "n_bit_mismatch": int(np.count_nonzero(phi != phi_o)), "unreached_match": same_inf,
+            "n_bit_mismatch": int(np.count_nonzero(phi != phi_o)),
+            "n_over_1e-4": int(np.count_nonzero(d > 1e-4 * tmax)), "unreached_match": same_inf,
             "tolerance": tolerance}
 
 
