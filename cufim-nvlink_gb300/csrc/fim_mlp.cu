@@ -42,8 +42,10 @@ namespace {
 // its tensor memory.
 //
 // umma_gemm_kernel (the weight gradients: M <= 128, long K): one CTA of four
-// warps per 128-row tile.  Warp 0 (one lane) streams the K slices of A and B
-// through a ring of kGemmStages stages (full/empty mbarriers); warp 1 (one
+// warps per 128-row tile and split of K (a long K is split over up to 32
+// CTAs, whose partial sums split_sum_kernel adds in a fixed order).  Warp 0
+// (one lane) streams the K slices of A and B through a ring of kGemmStages
+// stages (full/empty mbarriers); warp 1 (one
 // lane) issues four tcgen05.mma (M = N = 128, K = 16) per slice and commits
 // each slice's MMAs to the stage's empty barrier, the last one to the done
 // barrier; warp 2 owns the 128 tensor-memory columns of the accumulator; all
@@ -55,6 +57,8 @@ constexpr int kGemmStages = 3;
 constexpr uint32_t kGemmTileBytes = kGemmM * kGemmK * 2;  // one operand's slice: 16 KB (N == M)
 constexpr int kGemmSmem = kGemmStages * 2 * kGemmTileBytes + 1024;  // + slack to align the ring to 1024 B
 constexpr uint64_t kGemmWaitNs = 2000000000ull;  // bound of every mbarrier wait
+constexpr int kGemmSplitSlices = 4;   // K slices per CTA of a split weight-gradient GEMM (at least)
+constexpr int kGemmMaxSplits = 32;    // CTAs per 128-row tile at most
 static_assert(kGemmN == kGemmM, "the ring holds equal A and B slices");
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p)
@@ -166,7 +170,8 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi)
 
 __global__ void __launch_bounds__(128, 1) umma_gemm_kernel(const __grid_constant__ CUtensorMap ta,
                                                            const __grid_constant__ CUtensorMap tb, int M, int K,
-                                                           float *out32, int ldc, unsigned int *err)
+                                                           int kps, float *out32, int ldc, size_t split_stride,
+                                                           unsigned int *err)
 {
   extern __shared__ __align__(1024) unsigned char gemm_smem[];
   __shared__ __align__(8) uint64_t full_bar[kGemmStages], empty_bar[kGemmStages], done_bar;
@@ -175,7 +180,10 @@ __global__ void __launch_bounds__(128, 1) umma_gemm_kernel(const __grid_constant
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint32_t ring = (smem_u32(gemm_smem) + 1023u) & ~1023u;
   const int m0 = blockIdx.x * kGemmM;
-  const int nk = K / kGemmK;
+  // split blockIdx.y of K: slices [k0, k0 + nk), its partial sums at out32 + blockIdx.y * split_stride
+  const int k0 = blockIdx.y * kps;
+  const int nk = min(kps, K / kGemmK - k0);
+  out32 += blockIdx.y * split_stride;
   if (threadIdx.x == 0) {
     for (int s = 0; s < kGemmStages; ++s) {
       mbar_init(smem_u32(&full_bar[s]), 1);
@@ -209,8 +217,8 @@ __global__ void __launch_bounds__(128, 1) umma_gemm_kernel(const __grid_constant
       if (!mbar_wait(smem_u32(&empty_bar[s]), ph ^ 1u)) { s_fail = 1; break; }
       const uint32_t fb = smem_u32(&full_bar[s]);
       mbar_expect_tx(fb, 2 * kGemmTileBytes);
-      tma_load_2d(ring + s * kGemmTileBytes, &ta, i * kGemmK, m0, fb);
-      tma_load_2d(ring + (kGemmStages + s) * kGemmTileBytes, &tb, i * kGemmK, 0, fb);
+      tma_load_2d(ring + s * kGemmTileBytes, &ta, (k0 + i) * kGemmK, m0, fb);
+      tma_load_2d(ring + (kGemmStages + s) * kGemmTileBytes, &tb, (k0 + i) * kGemmK, 0, fb);
       issued = i + 1;
     }
   } else if (warp == 1 && lane == 0) {
@@ -557,10 +565,31 @@ bool make_map(CUtensorMap *map, const void *base, uint64_t k, uint64_t rows, uin
 
 }  // namespace
 
+namespace {
+// out[r][c] = sum over the splits, in split order (deterministic), of the
+// partial sums ws[s][r][c] (row stride ldc, split stride M * ldc)
+__global__ void split_sum_kernel(int M, int ldc, int splits, const float *__restrict__ ws, float *out)
+{
+  const int n = M * kGemmN;
+  const size_t st = (size_t)M * ldc;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int r = i / kGemmN, c = i % kGemmN;
+    const float *p = ws + (size_t)r * ldc + c;
+    float acc = 0.f;
+#pragma unroll 8
+    for (int s = 0; s < splits; ++s) acc += p[s * st];
+    out[(size_t)r * ldc + c] = acc;
+  }
+}
+}  // namespace
+
 // Weight gradients: C[M x 128] = A[M x K] B[128 x K]^T (FP32 out) for BF16
 // A (rows_a >= M rows) and B (128 rows), both with K contiguous, K a
-// multiple of 64 (the K loop of umma_gemm_kernel).
-cudaError_t mlp_gemm_wgrad(int M, int K, const void *A, int rows_a, const void *B, float *out32, int ldc,
+// multiple of 64 (the K loop of umma_gemm_kernel).  A long K is split over
+// up to kGemmMaxSplits CTAs per 128-row tile (kGemmSplitSlices K slices
+// each, partial sums in ws, which holds kGemmMaxSplits * M * ldc floats) and
+// summed in split order; without ws one CTA per tile runs the whole K.
+cudaError_t mlp_gemm_wgrad(int M, int K, const void *A, int rows_a, const void *B, float *out32, int ldc, float *ws,
                            unsigned int *err, cudaStream_t st)
 {
   if (M <= 0 || K <= 0 || K % kGemmK || rows_a < M) return cudaErrorInvalidValue;
@@ -570,7 +599,20 @@ cudaError_t mlp_gemm_wgrad(int M, int K, const void *A, int rows_a, const void *
   cudaError_t e;
   if ((e = cudaFuncSetAttribute(umma_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kGemmSmem)) !=
       cudaSuccess) return e;
-  umma_gemm_kernel<<<dim3((M + kGemmM - 1) / kGemmM), 128, kGemmSmem, st>>>(ta, tb, M, K, out32, ldc, err);
+  const int nk = K / kGemmK;
+  int kps = nk, splits = 1;
+  if (ws && nk > kGemmSplitSlices) {
+    kps = std::max(kGemmSplitSlices, (nk + kGemmMaxSplits - 1) / kGemmMaxSplits);
+    splits = (nk + kps - 1) / kps;
+  }
+  const dim3 grid((M + kGemmM - 1) / kGemmM, splits);
+  if (splits == 1) {
+    umma_gemm_kernel<<<grid, 128, kGemmSmem, st>>>(ta, tb, M, K, kps, out32, ldc, 0, err);
+    return cudaGetLastError();
+  }
+  umma_gemm_kernel<<<grid, 128, kGemmSmem, st>>>(ta, tb, M, K, kps, ws, ldc, (size_t)M * ldc, err);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  split_sum_kernel<<<(M * kGemmN + 255) / 256, 256, 0, st>>>(M, ldc, splits, ws, out32);
   return cudaGetLastError();
 }
 
@@ -838,6 +880,7 @@ struct fim_mlp {
   __nv_bfloat16 *H1 = nullptr, *H2 = nullptr, *H3 = nullptr, *dA = nullptr, *dB = nullptr;
   __nv_bfloat16 *HT = nullptr, *DT = nullptr;     // [kMlpH x cap] transposes for the weight gradients
   float *y = nullptr, *dy = nullptr;
+  float *ws = nullptr;                             // split-K partial sums of the weight gradients
   int64_t steps = 0;
 };
 
@@ -943,7 +986,7 @@ cudaError_t mlp_backward(fim_mlp *m, int n, const void *X)
   // layer 3
   if ((e = mlp_transpose(n, kMlpH, m->H2, m->HT, m->st)) != cudaSuccess) return e;
   if ((e = mlp_transpose(n, kMlpH, m->dA, m->DT, m->st)) != cudaSuccess) return e;
-  if ((e = mlp_gemm_wgrad(kMlpH, n, m->HT, kMlpH, m->DT, G + kMlpOW3, kMlpH, m->err, m->st)) != cudaSuccess) return e;
+  if ((e = mlp_gemm_wgrad(kMlpH, n, m->HT, kMlpH, m->DT, G + kMlpOW3, kMlpH, m->ws, m->err, m->st)) != cudaSuccess) return e;
   colsum_kernel<<<blocks, kMlpH, 0, m->st>>>(n, m->dA, G + kMlpOB3);
   RowEpi xm;
   xm.mask = m->H2; xm.out16 = m->dB;
@@ -951,7 +994,7 @@ cudaError_t mlp_backward(fim_mlp *m, int n, const void *X)
   // layer 2
   if ((e = mlp_transpose(n, kMlpH, m->H1, m->HT, m->st)) != cudaSuccess) return e;
   if ((e = mlp_transpose(n, kMlpH, m->dB, m->DT, m->st)) != cudaSuccess) return e;
-  if ((e = mlp_gemm_wgrad(kMlpH, n, m->HT, kMlpH, m->DT, G + kMlpOW2, kMlpH, m->err, m->st)) != cudaSuccess) return e;
+  if ((e = mlp_gemm_wgrad(kMlpH, n, m->HT, kMlpH, m->DT, G + kMlpOW2, kMlpH, m->ws, m->err, m->st)) != cudaSuccess) return e;
   colsum_kernel<<<blocks, kMlpH, 0, m->st>>>(n, m->dB, G + kMlpOB2);
   xm.mask = m->H1; xm.out16 = m->dA;
   if ((e = mlp_gemm_rows(kEpiMask, n, kMlpH, m->dB, m->W16 + kMlpOW2, xm, m->err, m->st)) != cudaSuccess) return e;
@@ -959,7 +1002,7 @@ cudaError_t mlp_backward(fim_mlp *m, int n, const void *X)
   // only reach output rows that are not stored
   if ((e = mlp_transpose(n, kMlpIn, X, m->HT, m->st)) != cudaSuccess) return e;
   if ((e = mlp_transpose(n, kMlpH, m->dA, m->DT, m->st)) != cudaSuccess) return e;
-  if ((e = mlp_gemm_wgrad(kMlpIn, n, m->HT, kMlpH, m->DT, G + kMlpOW1, kMlpH, m->err, m->st)) != cudaSuccess) return e;
+  if ((e = mlp_gemm_wgrad(kMlpIn, n, m->HT, kMlpH, m->DT, G + kMlpOW1, kMlpH, m->ws, m->err, m->st)) != cudaSuccess) return e;
   colsum_kernel<<<blocks, kMlpH, 0, m->st>>>(n, m->dA, G + kMlpOB1);
   return cudaGetLastError();
 }
@@ -1008,6 +1051,7 @@ extern "C" int fim_mlp_create(int device, uint64_t seed, fim_mlp **out)
       (e = cudaMalloc(&m->W16, sizeof(__nv_bfloat16) * kMlpW16)) != cudaSuccess ||
       (e = cudaMalloc(&m->W16T, sizeof(__nv_bfloat16) * kMlpW16)) != cudaSuccess ||
       (e = cudaMalloc(&m->err, sizeof(unsigned int))) != cudaSuccess ||
+      (e = cudaMalloc(&m->ws, sizeof(float) * kGemmMaxSplits * kMlpH * kMlpH)) != cudaSuccess ||
       (e = cudaMemset(m->err, 0, sizeof(unsigned int))) != cudaSuccess)
     return fail(mlp_fail("fim_mlp_create", e));
   // He initialisation (fixed seed); padded input rows and biases zero
@@ -1032,7 +1076,7 @@ extern "C" int fim_mlp_destroy(fim_mlp *m)
   if (m->st) cudaStreamSynchronize(m->st);
   mlp_free_acts(m);
   cudaFree(m->P); cudaFree(m->G); cudaFree(m->M); cudaFree(m->V); cudaFree(m->loss); cudaFree(m->W16);
-  cudaFree(m->W16T); cudaFree(m->err);
+  cudaFree(m->W16T); cudaFree(m->err); cudaFree(m->ws);
   if (m->st) cudaStreamDestroy(m->st);
   delete m;
   return FIM_OK;
